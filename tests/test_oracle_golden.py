@@ -1,0 +1,115 @@
+"""Pin the CPU oracle against outputs of the reference's own kernels.
+
+The fixtures were produced by tests/golden/make_golden.py, which executes
+Single_phase/LBM_3D_SinglePhase_Solver.py and 2phase/lbm_solver_3d_2phase_sparse.py
+unmodified (through a numpy stand-in for Taichi).  Single-phase agreement is
+bit-exact.  Two-phase agreement is bit-exact when the oracle replays the serial
+order of the reference's colour push (the reference's own GPU run sums it with
+atomics in no fixed order); in the oracle's deterministic slot order the
+difference is FP32 reordering noise, bounded below.
+"""
+import numpy as np
+import pytest
+
+from oracle.oracle import Oracle, make_params
+from tests import goldens as G
+
+
+@pytest.mark.parametrize("name", G.SP_CASES)
+def test_single_phase_bit_exact(name):
+    d = G.load(name)
+    o = Oracle(G.oracle_params(d), d["solid"])
+    fluid = d["solid"] == 0
+    done = 0
+    for st in d["steps"]:
+        o.step(int(st) - done)
+        done = int(st)
+        rho = o.field("rho").astype(np.float32)
+        v = o.field("v").astype(np.float32)
+        assert np.array_equal(rho[fluid], d["rho_%d" % st][fluid]), (name, st)
+        assert np.array_equal(v[fluid], d["v_%d" % st][fluid]), (name, st)
+        # solid cells: rho=1, v=0 (streaming3 else-branch)
+        assert np.all(rho[~fluid] == 1.0) and np.all(v[~fluid] == 0.0)
+
+
+def test_cavity50_fixture_geometry_and_first_step():
+    d = G.load("sp_cavity50")
+    solid = G.cavity_solid_50()
+    # geo_cavity.dat as the reference's init_geo loaded it: solid shell except the x=49 face
+    exp = np.zeros((50, 50, 50), np.int8)
+    exp[0] = 1
+    exp[:, 0] = 1
+    exp[:, -1] = 1
+    exp[:, :, 0] = 1
+    exp[:, :, -1] = 1
+    assert np.array_equal(solid, exp)
+    assert int(d["n_solid"]) == int(exp.sum())
+    P = G.params_of(d)
+    o = Oracle(make_params((50, 50, 50), niu=P["niu"], bc=P["bc"], rho_bc=P["rho_bc"], vel_bc=P["vel_bc"]), solid)
+    o.step(1)
+    fl = solid == 0
+    assert np.array_equal(o.field("rho").astype(np.float32)[fl], d["rho_1"][fl])
+    assert np.array_equal(o.field("v").astype(np.float32)[fl], d["v_1"][fl])
+
+
+@pytest.mark.parametrize("name", G.TP_CASES)
+def test_two_phase_bit_exact_in_reference_order(name):
+    d = G.load(name)
+    o = Oracle(G.oracle_params(d, ref_emulation=3), d["solid"], d["psi0"])
+    fluid = d["solid"] == 0
+    done = 0
+    for st in d["steps"]:
+        o.step(int(st) - done)
+        done = int(st)
+        for f in ("rho", "v", "psi", "rho_r", "rho_b"):
+            a = o.field(f).astype(np.float32)
+            assert np.array_equal(a[fluid], d["%s_%d" % (f, st)][fluid]), (name, st, f)
+
+
+@pytest.mark.parametrize("name", G.TP_CASES)
+def test_two_phase_deterministic_order_within_tolerance(name):
+    d = G.load(name)
+    o = Oracle(G.oracle_params(d, ref_emulation=0), d["solid"], d["psi0"])
+    fluid = d["solid"] == 0
+    st = int(d["steps"][-1])
+    o.step(st)
+    for f, tol in (("rho", 2e-6), ("psi", 2e-6), ("rho_r", 2e-6), ("rho_b", 2e-6), ("v", 2e-4)):
+        err = G.normwise_rel(o.field(f), d["%s_%d" % (f, st)], fluid)
+        assert err < tol, (name, f, err)
+
+
+def test_stream_permutation_matches_reference():
+    d = G.load("sp_stream")
+    shape = tuple(int(x) for x in d["shape"])
+    o = Oracle(make_params(shape), d["solid"])
+    o.set_field("f", d["f_in"])
+    o.set_field("F", np.full(shape + (19,), np.nan))
+    o.stream_only()
+    F = o.field("F").astype(np.float32)
+    fluid = d["solid"] == 0
+    assert np.array_equal(F[fluid], d["F_out"][fluid])
+
+
+def test_inverse_moment_matrix_is_fp32_of_exact_inverse():
+    from fractions import Fraction
+    import sympy
+    o = Oracle(make_params((3, 3, 3)), np.zeros((3, 3, 3), np.int8))
+    inv = o.inv_m()
+    from tests.test_host_tables import M_REF
+    exact = sympy.Matrix(M_REF.tolist()).inv()
+    for r in range(19):
+        for c in range(19):
+            e = float(Fraction(int(exact[r, c].p), int(exact[r, c].q)))
+            assert np.float32(inv[r, c]) == np.float32(e)
+
+
+def test_fp64_oracle_close_to_fp32():
+    d = G.load("sp_mixed")
+    p = G.oracle_params(d)
+    a = Oracle(p, d["solid"], precision=32)
+    b = Oracle(p, d["solid"], precision=64)
+    a.step(10)
+    b.step(10)
+    fl = d["solid"] == 0
+    assert G.normwise_rel(a.field("rho"), b.field("rho"), fl) < 1e-6
+    assert G.normwise_rel(a.field("v"), b.field("v"), fl) < 1e-4
