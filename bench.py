@@ -1,0 +1,313 @@
+"""Benchmark of the fused D3Q19 MRT step on GB300.
+
+Workload (single GPU): single-phase porous flow on a 256^3 seeded sphere pack
+(radii U[4,10], porosity 0.35, percolating cluster only), fixed pressure
+rho = 1.0005 / 1.0 on the x faces, periodic y/z, niu = 0.1, FP32 populations.
+A "step" is one lattice time step over that lattice (one kernel launch).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line.  ``value`` = fluid-node MLUPS with the state resident in
+HBM, timed with CUDA events on the library's stream; ``e2e`` = the same metric
+through the public solver class with host buffers (geometry upload, init, K
+steps, rho/v download inside the timed region); ``roofline`` = algorithmic
+bytes (152 B per fluid node per step) / launch time against the measured HBM
+copy bandwidth; ``cpu_baseline`` = the CPU oracle (the reference's four-sweep
+algorithm in C/OpenMP) on a bounded sample of the same workload.
+``--impl reference`` times that CPU implementation alone on all host threads.
+Under torchrun (N > 1) every rank runs its own replica (the path is replicated,
+not sharded: there is no exchange step).
+"""
+import argparse
+import json
+import os
+import re
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SHAPE = (256, 256, 256)
+PACK = dict(rmin=4.0, rmax=10.0, porosity=0.35, seed=2)
+RHO_IN, RHO_OUT, NIU = 1.0005, 1.0, 0.1
+BYTES_PER_NODE = {"f32": 152, "f16": 76, "bf16": 76, "f64": 304}
+METRIC = "MLUPS"
+UNIT = "MLUPS (1e6 fluid-node updates per second)"
+PROFILE_MD = os.path.join(ROOT, "profiles", "sp_step_kernel_f32_porous256.md")
+
+
+def workload_config(storage="f32"):
+    return {"workload": "single-phase D3Q19 MRT step, 256^3 sphere pack (r U[4,10], phi 0.35, seed 2, "
+                        "percolating), pressure x 1.0005/1.0, periodic y/z, niu 0.1",
+            "lattice": list(SHAPE), "storage": storage, "steps_per_launch": 1,
+            "l2": "inputs larger than L2 (populations ~0.9 GB per step vs 129 MB L2), no flush",
+            "parallelism": "replicas"}
+
+
+def geometry():
+    from taichi_lbm3d_gb300.geometry import sphere_pack
+    return sphere_pack(SHAPE, PACK["rmin"], PACK["rmax"], PACK["porosity"], PACK["seed"])
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic_per_node():
+    """dram bytes per fluid node per launch from the committed ncu summary."""
+    try:
+        txt = open(PROFILE_MD).read()
+        m = re.search(r"dram_bytes_per_fluid_node:\s*([0-9.]+)", txt)
+        return float(m.group(1)) if m else None
+    except OSError:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 100 ms."""
+    Q = ("timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.samples = []
+        self.proc = None
+        self.index = index
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append((time.time(), line.strip()))
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self, t0, t1):
+        rows = [s for t, s in self.samples if t0 <= t <= t1] or [s for _, s in self.samples[-3:]]
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            f = [x.strip() for x in r.split(",")]
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except (ValueError, IndexError):
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def time_device(lat, steps, warmup):
+    """Warm up, then time `steps` launches with CUDA events on the library stream."""
+    import torch
+    stream = torch.cuda.ExternalStream(lat.stream())
+    lat.step_async(warmup)
+    lat.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    lat.step_async(steps)
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / 1e3
+
+
+def run_variant(solid, storage, steps, warmup):
+    from taichi_lbm3d_gb300 import _native
+    p = _native.make_params(SHAPE, niu=NIU, bc=(1, 1, 0, 0, 0, 0), rho_bc=(RHO_IN, RHO_OUT, 1, 1, 1, 1),
+                            storage=storage)
+    lat = _native.Lattice(p)
+    lat.set_geometry(solid)
+    lat.init()
+    secs = time_device(lat, steps, warmup)
+    nf = lat.info().n_fluid
+    lat.close()
+    return nf, secs
+
+
+def e2e_run(solid, steps):
+    """Same metric through the public class, host buffers in and out."""
+    from taichi_lbm3d_gb300 import LB3D_Solver_Single_Phase
+    t0 = time.perf_counter()
+    lb = LB3D_Solver_Single_Phase(*SHAPE)
+    lb.solid.from_numpy(solid)
+    lb.set_viscosity(NIU)
+    lb.set_bc_rho_x0(RHO_IN)
+    lb.set_bc_rho_x1(RHO_OUT)
+    lb.init_simulation()
+    lb.run(steps)
+    rho = lb.rho.to_numpy()
+    v = lb.v.to_numpy()
+    secs = time.perf_counter() - t0
+    nf = lb.n_fluid
+    lb.close()
+    np_pad = (nf + 63) // 64 * 64
+    h2d = solid.size * 1 + 4 * solid.size + 4 * np_pad          # mask, neighbour map, coordinates
+    d2h = 16 * np_pad                                            # rho + v of the fluid nodes
+    assert np.isfinite(rho).all() and np.isfinite(v).all()
+    return nf * steps / secs / 1e6, h2d / steps, d2h / steps
+
+
+def cpu_baseline(solid, max_seconds=20.0):
+    """The CPU oracle (reference algorithm: 4 sweeps, AoS, OpenMP) on this
+    workload for a bounded number of steps."""
+    from oracle.oracle import Oracle, make_params
+    cores = len(os.sched_getaffinity(0))
+    p = make_params(SHAPE, niu=NIU, bc=(1, 1, 0, 0, 0, 0), rho_bc=(RHO_IN, RHO_OUT, 1, 1, 1, 1))
+    o = Oracle(p, solid)
+    o.step(1)                       # warm-up (page-in)
+    nf = int((solid == 0).sum())
+    n, t = 0, 0.0
+    while t < max_seconds and n < 200:
+        t0 = time.perf_counter()
+        o.step(1)
+        t += time.perf_counter() - t0
+        n += 1
+    o.close()
+    return {"value": nf * n / t / 1e6, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "%d steps of the full 256^3 workload (%.1f s)" % (n, t)}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-variants", action="store_true")
+    a = ap.parse_args()
+    warmup = max(3, a.warmup)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if a.impl == "reference":
+        if rank != 0:
+            return 0
+        solid = geometry()
+        cb = cpu_baseline(solid, max_seconds=min(120.0, 3.0 * max(1, a.steps)))
+        line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": a.gpus,
+                "steps": int(re.match(r"(\d+)", cb["sample"]).group(1)), "warmup": 1,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded sphere pack)", "config": workload_config(),
+                "cpu_baseline": cb,
+                "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                "note": "the reference's Taichi ti.cpu path is not installable offline; this is the C oracle "
+                        "restating its four-sweep algorithm"}
+        print(json.dumps(line))
+        return 0
+
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+
+    solid = geometry()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+
+    from taichi_lbm3d_gb300 import _native
+    p = _native.make_params(SHAPE, niu=NIU, bc=(1, 1, 0, 0, 0, 0), rho_bc=(RHO_IN, RHO_OUT, 1, 1, 1, 1),
+                            storage="f32", device=local)
+    lat = _native.Lattice(p)
+    lat.set_geometry(solid)
+    lat.init()
+    nf = lat.info().n_fluid
+    stream = torch.cuda.ExternalStream(lat.stream())
+    lat.step_async(warmup)
+    lat.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    t_wall0 = time.time()
+    e0.record(stream)
+    lat.step_async(a.steps)
+    e1.record(stream)
+    e1.synchronize()
+    t_wall1 = time.time()
+    torch.cuda.synchronize()
+    secs = e0.elapsed_time(e1) / 1e3
+    st = lat.stats()
+    lat.close()
+    if world > 1:
+        t = torch.tensor([secs], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        secs = float(t.item())
+        torch.distributed.barrier()
+    clocks.stop()
+    clk = clocks.summary(t_wall0, t_wall1)
+
+    mlups = nf * a.steps * world / secs / 1e6
+    per_launch = secs / a.steps
+    peak, peak_kind = measured_peak()
+    achieved = BYTES_PER_NODE["f32"] * nf / per_launch / 1e9
+    tpn = profiled_traffic_per_node()
+    line = {
+        "metric": METRIC, "value": mlups, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": warmup,
+        "ms_per_step": per_launch * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded sphere pack, numpy default_rng seed 2)",
+        "config": dict(workload_config(), n_fluid=nf, porosity_after_percolation=float(nf) / solid.size),
+        "clocks": clk, "gpu_launches": a.steps,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind,
+                     "traffic": (tpn * nf) if tpn else None,
+                     "algorithmic_bytes_per_node": BYTES_PER_NODE["f32"]},
+        "checks": {"mass": st.mass, "n_nonfinite": st.n_nonfinite},
+    }
+    if rank == 0:
+        if not a.no_variants:
+            var = {}
+            for sto in ("f16", "bf16"):
+                nfv, sv = run_variant(solid, sto, min(a.steps, 1000), warmup)
+                var[sto] = {"value": nfv * min(a.steps, 1000) / sv / 1e6, "unit": UNIT,
+                            "gbs_algorithmic": BYTES_PER_NODE[sto] * nfv * min(a.steps, 1000) / sv / 1e9}
+            line["variants"] = var
+        e2e, h2d, d2h = e2e_run(solid, a.steps)
+        line["e2e"] = {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                       "path": "LB3D_Solver_Single_Phase: solid.from_numpy, init_simulation, run(K), "
+                               "rho/v to_numpy, host wall clock"}
+        if not a.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(solid)
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,173 @@
+/* lbm_gb300.h -- C ABI of the GB300-native D3Q19 MRT lattice Boltzmann hot path.
+ *
+ * The library (taichi_lbm3d_gb300/liblbm_gb300.so) implements one time step of
+ * taichi_LBM3D's solvers as fused sm_103a CUDA kernels over a compacted list of
+ * fluid nodes.  It replaces the Taichi kernels that the reference's Python
+ * solver classes launch; each entry point names the reference interface it
+ * stands in for (paths inside the taichi_LBM3D tree):
+ *
+ *   SP = Single_phase/LBM_3D_SinglePhase_Solver.py
+ *   TP = 2phase/lbm_solver_3d_2phase_sparse.py
+ *
+ * Conventions
+ *   - Every call returns 0 on success or a negative LBM_E* code; the message of
+ *     the last failure is available from lbm_last_error().
+ *   - Host arrays are caller-owned, dense over the lattice, cell order x fastest:
+ *     cell = i + nx*(j + ny*k)  (the order of the reference's geometry files,
+ *     SP:173-177).  Vector fields are interleaved: v[cell*3 + c].
+ *   - A handle owns its device memory and one CUDA stream; use a handle from one
+ *     host thread at a time.  Calls are synchronous unless named *_async.
+ *   - There is no CPU fallback: lbm_create fails with LBM_ENODEV when no CUDA
+ *     device of compute capability 10.3 (GB300) is present.
+ */
+#ifndef LBM_GB300_H
+#define LBM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LBM_ABI_VERSION 1
+
+enum {
+    LBM_OK = 0,
+    LBM_EINVAL = -1,   /* bad argument / parameter */
+    LBM_ENODEV = -2,   /* no usable sm_103 device */
+    LBM_ENOMEM = -3,   /* device or host allocation failed */
+    LBM_ECUDA = -4,    /* CUDA runtime error */
+    LBM_ESTATE = -5,   /* call out of order (e.g. step before geometry) */
+    LBM_EDIVERGED = -6 /* NaN/Inf detected by a reduction */
+};
+
+/* Boundary codes per face (SP:22-28): 0 periodic, 1 fixed pressure, 2 fixed velocity.
+ * Face order everywhere: x-left, x-right, y-left, y-right, z-left, z-right. */
+enum { LBM_BC_PERIODIC = 0, LBM_BC_PRESSURE = 1, LBM_BC_VELOCITY = 2 };
+
+/* Population storage of the fused kernels. */
+enum {
+    LBM_STORE_F32 = 0,       /* plain FP32 populations */
+    LBM_STORE_F16_DEV = 1,   /* FP16 of (f_s - w_s)*2^12, collide in FP32 */
+    LBM_STORE_BF16_DEV = 2,  /* BF16 of (f_s - w_s), collide in FP32 */
+    LBM_STORE_F64 = 3        /* FP64 populations and arithmetic (accuracy reference) */
+};
+
+/* Solver parameters: the attributes the reference's class sets before
+ * init_simulation() (SP:11-28, :118-149) and the two-phase script's module
+ * globals (TP:17-40).  Doubles are Python floats; the kernels round them to
+ * the compute type exactly as Taichi folds Python constants. */
+typedef struct LbmParams {
+    int32_t nx, ny, nz;
+    int32_t bc[6];
+    double rho_bc[6];
+    double vel_bc[6][3];
+    double niu;
+    double force[3];
+    int32_t visc_convention; /* 0: tau = niu/3+0.5 (SP:127); 1: tau = 3*niu+0.5 (scripts, TP:104) */
+    int32_t guo_convention;  /* 0: class Guo term /3, /9 (SP:236); 1: script form (TP:246); 2: standard 3, 9 */
+    int32_t bc_form;         /* velocity faces: 0 feq(s,1,u) (SP:288); 1 in-place form (TP:506) */
+    int32_t storage;         /* LBM_STORE_* */
+    int32_t two_phase;       /* 0 single phase (SP), 1 colour-gradient two phase (TP) */
+    double niu_l, niu_g, psi_solid, cap_a;  /* TP:22-25 */
+    int32_t psi_bc[6];       /* TP:35-40: 0 periodic, 1 constant psi */
+    double psi_val[6];
+    int32_t device;          /* CUDA device ordinal */
+    int32_t block_size;      /* threads per CTA of the step kernel, 0 = default */
+} LbmParams;
+
+typedef struct LbmInfo {
+    int64_t n_cells;
+    int64_t n_fluid;
+    int64_t steps_done;
+    int64_t device_bytes;    /* bytes of device memory held by the handle */
+    int32_t storage;
+    int32_t two_phase;
+    int32_t sm_count;
+    int32_t abi_version;
+} LbmInfo;
+
+/* FP64 reductions over the fluid nodes of the last completed step. */
+typedef struct LbmStats {
+    double mass;             /* sum of rho */
+    double mom[3];           /* sum of v (not rho*v), per component */
+    double max_v;            /* max |v| over fluid nodes (solid cells have v = 0) */
+    int64_t n_nonfinite;     /* rho or v not finite */
+    int64_t n_fluid;
+} LbmStats;
+
+typedef struct LbmHandle LbmHandle;
+
+int lbm_abi_version(void);
+
+/* Stands in for LB3D_Solver_Single_Phase.__init__ (SP:11-114) plus the field
+ * allocation that Taichi does; two-phase: the module-level allocations (TP:53-96). */
+int lbm_create(const LbmParams* params, LbmHandle** out);
+int lbm_destroy(LbmHandle* h);
+
+/* Geometry: solid[cell] > 0 is solid (init_geo, SP:173-177; solid.from_numpy in
+ * example_poiseuille_flow.py:24).  Builds the compacted fluid index and the
+ * neighbour map on the device.  The lattice size is the one in LbmParams. */
+int lbm_set_geometry(LbmHandle* h, const int8_t* solid);
+
+/* Two-phase initial phase field psi[cell] (TP:195-203, psi.from_numpy). */
+int lbm_set_psi(LbmHandle* h, const float* psi);
+
+/* Initial state: rho = 1, v = 0, f = feq (init, SP:160-170 / TP:174-187) when
+ * rho and v are NULL; otherwise f = feq(rho, v) from the given dense fields
+ * (the warm start).  Resets the step counter. */
+int lbm_init(LbmHandle* h, const float* rho, const float* v);
+
+/* Advance n time steps (SP:477-481 step(); TP:626-632).  lbm_step waits for the
+ * GPU; lbm_step_async only enqueues on the handle's stream. */
+int lbm_step(LbmHandle* h, int32_t n);
+int lbm_step_async(LbmHandle* h, int32_t n);
+int lbm_synchronize(LbmHandle* h);
+
+/* The handle's CUDA stream (cudaStream_t), for event timing by the caller. */
+int lbm_get_stream(LbmHandle* h, void** stream);
+
+/* rho / v after the last step, dense (SP:470-473 to_numpy); solid cells hold
+ * rho = 1, v = 0 (SP:390-392).  Either pointer may be NULL. */
+int lbm_get_macros(LbmHandle* h, float* rho, float* v);
+
+/* Same as lbm_get_macros in FP64 (exact for LBM_STORE_F64 handles; FP32 values
+ * widened otherwise): the accuracy-reference readback. */
+int lbm_get_macros_f64(LbmHandle* h, double* rho, double* v);
+
+/* Two-phase fields after the last step: psi, rho_r, rho_b (dense; NULL to skip). */
+int lbm_get_phase(LbmHandle* h, float* psi, float* rho_r, float* rho_b);
+
+/* get_max_v / cal_max_v (SP:394-402): max |v| over all cells. */
+int lbm_get_max_v(LbmHandle* h, float* out);
+
+/* FP64 reductions (mass, momentum, max |v|, non-finite count). */
+int lbm_reductions(LbmHandle* h, LbmStats* out);
+
+int lbm_get_info(LbmHandle* h, LbmInfo* out);
+
+/* Compacted fluid index: cell id of each fluid node, in node order (n_fluid). */
+int lbm_get_fluid_index(LbmHandle* h, int32_t* cell_of_node);
+
+/* Pull sources of the neighbour table, [18][n_fluid] for directions 1..18:
+ * the node pulled from (x - e_s, periodic wrap of SP:247-257), or -1 - node
+ * when that cell is solid (halfway bounce-back from the node's own LR slot). */
+int lbm_get_neighbors(LbmHandle* h, int32_t* src);
+
+/* Populations in node order, [19][n_fluid] as FP64 (checkpoint / tests). */
+int lbm_get_populations(LbmHandle* h, double* f);
+int lbm_set_populations(LbmHandle* h, const double* f);
+
+/* One pull-stream of given populations with identity collision and no
+ * boundary condition (streaming1, SP:259-269): in/out [19][n_fluid] FP32. */
+int lbm_debug_stream(LbmHandle* h, const float* f_in, float* f_out);
+
+/* Copy the message of the last error on this handle (or the last global error
+ * when h is NULL) into buf. */
+int lbm_last_error(LbmHandle* h, char* buf, size_t n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LBM_GB300_H */

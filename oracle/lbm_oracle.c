@@ -31,7 +31,7 @@ typedef struct OracleParams {
     double niu;
     double force[3];
     int32_t visc_convention;  /* 0: tau = niu/3 + 0.5 (class, :127); 1: tau = 3 niu + 0.5 (scripts) */
-    int32_t guo_convention;   /* 0: class /3, /9 (:236); 1: script, no factors */
+    int32_t guo_convention;   /* 0: class /3, /9 (:236); 1: script, no factors; 2: standard 3, 9 */
     int32_t bc_form;          /* velocity faces: 0 class feq(s,1,u); 1 script in-place form */
     int32_t two_phase;
     double niu_l, niu_g, psi_solid, cap_a;

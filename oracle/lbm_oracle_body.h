@@ -199,7 +199,8 @@ static void FN(collide_sp_)(ST(oracle_sp_) *o) {
                     REAL ef = (REAL)E[l][0] * fv[0]; ef = ef + (REAL)E[l][1] * fv[1]; ef = ef + (REAL)E[l][2] * fv[2];
                     REAL g;
                     if (p->guo_convention == 0) g = a / (REAL)3.0 + (eu * ef) / (REAL)9.0;
-                    else g = a + eu * ef;
+                    else if (p->guo_convention == 1) g = a + eu * ef;
+                    else g = (REAL)3.0 * a + (REAL)9.0 * (eu * ef);  /* standard Guo (not in the reference) */
                     fg = fg + ((REAL)W[l] * g) * o->Mf[s][l];
                 }
                 m[s] = m[s] + ((REAL)1 - (REAL)0.5 * o->S[s]) * fg;

@@ -1,0 +1,537 @@
+// C ABI of liblbm_gb300.so (declared in include/lbm_gb300.h): handle
+// lifecycle, geometry / compacted index, initial state, stepping, readback.
+// The Python solver classes call these through ctypes.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "lbm_common.cuh"
+#include "lbm_internal.h"
+
+namespace {
+std::mutex g_err_mu;
+std::string g_err;
+
+int set_global_err(int code, const std::string& m) {
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    g_err = m;
+    return code;
+}
+
+template <typename T>
+int dev_alloc(LbmHandle* h, T** p, size_t bytes, const char* what) {
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc((void**)p, bytes);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return lbm_set_err(h, LBM_ENOMEM, std::string("cudaMalloc failed for ") + what + ": " + cudaGetErrorString(e));
+    }
+    h->device_bytes += (int64_t)bytes;
+    return LBM_OK;
+}
+
+template <typename T>
+void dev_free(T*& p) {
+    if (p) cudaFree((void*)p);
+    p = nullptr;
+}
+
+void free_lattice(LbmHandle* h) {
+    dev_free(h->d_map);
+    dev_free(h->d_coord);
+    dev_free(h->d_f[0]);
+    dev_free(h->d_f[1]);
+    dev_free(h->d_vprev);
+    dev_free(h->d_rho);
+    dev_free(h->d_v);
+    dev_free(h->d_psi);
+    dev_free(h->d_rr[0]);
+    dev_free(h->d_rr[1]);
+    dev_free(h->d_rb[0]);
+    dev_free(h->d_rb[1]);
+    dev_free(h->d_cg);
+    dev_free(h->d_psi_dense);
+    dev_free(h->d_red);
+    dev_free(h->d_red_out);
+    h->device_bytes = 0;
+}
+
+size_t store_elem(int storage) {
+    switch (storage) {
+    case LBM_STORE_F32: return 4;
+    case LBM_STORE_F16_DEV: return 2;
+    case LBM_STORE_BF16_DEV: return 2;
+    case LBM_STORE_F64: return 8;
+    }
+    return 0;
+}
+
+int validate(const LbmParams* p, std::string* why) {
+    char b[256];
+    if (p->nx < 1 || p->ny < 1 || p->nz < 1) { *why = "lattice size must be positive"; return LBM_EINVAL; }
+    if (p->nx > 2047 || p->ny > 2047 || p->nz > 1023) {
+        *why = "lattice too large: nx, ny <= 2047 and nz <= 1023 (packed node coordinates)";
+        return LBM_EINVAL;
+    }
+    if ((int64_t)p->nx * p->ny * p->nz >= (int64_t)1 << 31) { *why = "lattice has >= 2^31 cells"; return LBM_EINVAL; }
+    const int n[3] = {p->nx, p->ny, p->nz};
+    for (int f = 0; f < 6; ++f) {
+        if (p->bc[f] < 0 || p->bc[f] > 2) {
+            snprintf(b, sizeof b, "bc[%d]=%d: must be 0 (periodic), 1 (pressure) or 2 (velocity)", f, p->bc[f]);
+            *why = b;
+            return LBM_EINVAL;
+        }
+        if (p->bc[f] != 0 && n[f / 2] < 2) {
+            snprintf(b, sizeof b, "face %d has a non-periodic BC but the lattice is 1 cell thick there", f);
+            *why = b;
+            return LBM_EINVAL;
+        }
+        if (p->psi_bc[f] < 0 || p->psi_bc[f] > 1) { *why = "psi_bc must be 0 or 1"; return LBM_EINVAL; }
+    }
+    if (!(p->niu > 0) && !p->two_phase) { *why = "niu must be > 0"; return LBM_EINVAL; }
+    if (store_elem(p->storage) == 0) { *why = "unknown storage"; return LBM_EINVAL; }
+    if (p->visc_convention < 0 || p->visc_convention > 1 || p->guo_convention < 0 || p->guo_convention > 2 ||
+        p->bc_form < 0 || p->bc_form > 1) {
+        *why = "convention flags must be 0 or 1";
+        return LBM_EINVAL;
+    }
+    if (p->two_phase && (!(p->niu_l > 0) || !(p->niu_g > 0))) { *why = "niu_l and niu_g must be > 0"; return LBM_EINVAL; }
+    if (p->block_size != 0 && (p->block_size < 32 || p->block_size > 256 || p->block_size % 32)) {
+        *why = "block_size must be a multiple of 32 in [32, 256]";
+        return LBM_EINVAL;
+    }
+    return LBM_OK;
+}
+}  // namespace
+
+int lbm_set_err(LbmHandle* h, int code, const std::string& msg) {
+    if (h) h->err = msg;
+    set_global_err(code, msg);
+    return code;
+}
+
+int lbm_cuda_check(LbmHandle* h, cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return LBM_OK;
+    return lbm_set_err(h, LBM_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+extern "C" {
+
+int lbm_abi_version(void) { return LBM_ABI_VERSION; }
+
+int lbm_create(const LbmParams* params, LbmHandle** out) {
+    if (!params || !out) return set_global_err(LBM_EINVAL, "lbm_create: NULL argument");
+    *out = nullptr;
+    std::string why;
+    int rc = validate(params, &why);
+    if (rc) return set_global_err(rc, "lbm_create: " + why);
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return set_global_err(LBM_ENODEV, "lbm_create: no CUDA device (this library has no CPU path)");
+    if (params->device < 0 || params->device >= ndev) return set_global_err(LBM_EINVAL, "lbm_create: bad device ordinal");
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, params->device) != cudaSuccess)
+        return set_global_err(LBM_ENODEV, "lbm_create: cudaGetDeviceProperties failed");
+    if (!(prop.major == 10 && prop.minor == 3)) {
+        char b[160];
+        snprintf(b, sizeof b, "lbm_create: device %d is sm_%d%d; this library is built for sm_103a (GB300) only",
+                 params->device, prop.major, prop.minor);
+        return set_global_err(LBM_ENODEV, b);
+    }
+    LbmHandle* h = new LbmHandle();
+    h->p = *params;
+    h->device = params->device;
+    h->sm_count = prop.multiProcessorCount;
+    h->elem = store_elem(params->storage);
+    h->f64 = params->storage == LBM_STORE_F64;
+    h->force = params->force[0] != 0 || params->force[1] != 0 || params->force[2] != 0;
+    h->block = params->block_size ? params->block_size : 256;
+    h->ncell = (int64_t)params->nx * params->ny * params->nz;
+    cudaSetDevice(h->device);
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete h;
+        return set_global_err(LBM_ECUDA, "lbm_create: cudaStreamCreate failed");
+    }
+    *out = h;
+    return LBM_OK;
+}
+
+int lbm_destroy(LbmHandle* h) {
+    if (!h) return LBM_OK;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    free_lattice(h);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return LBM_OK;
+}
+
+// Compacted index: fluid nodes in cell order (x fastest), the order in which
+// the reference's block-sparse storage is activated by init (SP:160-170).
+int lbm_set_geometry(LbmHandle* h, const int8_t* solid) {
+    if (!h || !solid) return lbm_set_err(h, LBM_EINVAL, "lbm_set_geometry: NULL argument");
+    cudaSetDevice(h->device);
+    cudaStreamSynchronize(h->stream);
+    free_lattice(h);
+    h->have_geometry = h->initialized = h->macros_valid = false;
+    const int64_t nc = h->ncell;
+    h->solid.assign(solid, solid + nc);
+    std::vector<int32_t> map(nc);
+    h->cell_of_node.clear();
+    int32_t nf = 0;
+    for (int64_t c = 0; c < nc; ++c) {
+        if (solid[c] > 0) {
+            h->solid[c] = 1;
+            map[c] = -1;
+        } else {
+            h->solid[c] = 0;
+            map[c] = nf++;
+            h->cell_of_node.push_back((int32_t)c);
+        }
+    }
+    h->n_fluid = nf;
+    h->np = ((int64_t)std::max(nf, 1) + 63) / 64 * 64;
+    std::vector<uint32_t> coord(h->np, 0);
+    const int nx = h->p.nx, ny = h->p.ny;
+    for (int32_t n = 0; n < nf; ++n) {
+        const int64_t c = h->cell_of_node[n];
+        const int i = (int)(c % nx), j = (int)((c / nx) % ny), k = (int)(c / ((int64_t)nx * ny));
+        coord[n] = lbm_pack(i, j, k);
+    }
+    const size_t rbytes = h->f64 ? 8 : 4;
+    int rc = 0;
+    rc = rc ? rc : dev_alloc(h, &h->d_map, sizeof(int32_t) * nc, "map");
+    rc = rc ? rc : dev_alloc(h, &h->d_coord, sizeof(uint32_t) * h->np, "coord");
+    rc = rc ? rc : dev_alloc(h, &h->d_f[0], h->elem * 19 * h->np, "f_A");
+    rc = rc ? rc : dev_alloc(h, &h->d_f[1], h->elem * 19 * h->np, "f_B");
+    rc = rc ? rc : dev_alloc(h, &h->d_vprev, rbytes * 3 * h->np, "vprev");
+    rc = rc ? rc : dev_alloc(h, &h->d_rho, rbytes * h->np, "rho");
+    rc = rc ? rc : dev_alloc(h, &h->d_v, rbytes * 3 * h->np, "v");
+    if (!rc && h->p.two_phase) {
+        rc = rc ? rc : dev_alloc(h, &h->d_psi, rbytes * h->np, "psi");
+        rc = rc ? rc : dev_alloc(h, &h->d_rr[0], rbytes * h->np, "rho_r A");
+        rc = rc ? rc : dev_alloc(h, &h->d_rr[1], rbytes * h->np, "rho_r B");
+        rc = rc ? rc : dev_alloc(h, &h->d_rb[0], rbytes * h->np, "rho_b A");
+        rc = rc ? rc : dev_alloc(h, &h->d_rb[1], rbytes * h->np, "rho_b B");
+        rc = rc ? rc : dev_alloc(h, &h->d_cg, rbytes * 3 * h->np, "colour gradient");
+        rc = rc ? rc : dev_alloc(h, &h->d_psi_dense, sizeof(float) * nc, "psi dense");
+    }
+    h->red_blocks = (int)std::min<int64_t>(4 * h->sm_count, (h->n_fluid + 255) / 256 + 1);
+    rc = rc ? rc : dev_alloc(h, &h->d_red, sizeof(double) * 8 * h->red_blocks, "reduction partials");
+    rc = rc ? rc : dev_alloc(h, &h->d_red_out, sizeof(double) * 8, "reduction result");
+    if (rc) { free_lattice(h); return rc; }
+    rc = lbm_cuda_check(h, cudaMemcpyAsync(h->d_map, map.data(), sizeof(int32_t) * nc, cudaMemcpyHostToDevice, h->stream), "copy map");
+    if (!rc) rc = lbm_cuda_check(h, cudaMemcpyAsync(h->d_coord, coord.data(), sizeof(uint32_t) * h->np, cudaMemcpyHostToDevice, h->stream), "copy coord");
+    if (!rc) rc = lbm_cuda_check(h, cudaMemsetAsync(h->d_f[0], 0, h->elem * 19 * h->np, h->stream), "clear f");
+    if (!rc) rc = lbm_cuda_check(h, cudaMemsetAsync(h->d_f[1], 0, h->elem * 19 * h->np, h->stream), "clear f");
+    if (!rc) rc = lbm_cuda_check(h, cudaMemsetAsync(h->d_vprev, 0, rbytes * 3 * h->np, h->stream), "clear vprev");
+    if (!rc) rc = lbm_cuda_check(h, cudaStreamSynchronize(h->stream), "lbm_set_geometry");
+    if (rc) { free_lattice(h); return rc; }
+    h->have_geometry = true;
+    h->have_psi = false;
+    return LBM_OK;
+}
+
+int lbm_set_psi(LbmHandle* h, const float* psi) {
+    if (!h || !psi) return lbm_set_err(h, LBM_EINVAL, "lbm_set_psi: NULL argument");
+    if (!h->p.two_phase) return lbm_set_err(h, LBM_ESTATE, "lbm_set_psi: handle is single phase");
+    if (!h->have_geometry) return lbm_set_err(h, LBM_ESTATE, "lbm_set_psi: call lbm_set_geometry first");
+    h->psi0.assign(psi, psi + h->ncell);
+    h->have_psi = true;
+    h->initialized = false;
+    return LBM_OK;
+}
+
+int lbm_init(LbmHandle* h, const float* rho, const float* v) {
+    if (!h) return lbm_set_err(h, LBM_EINVAL, "lbm_init: NULL handle");
+    if (!h->have_geometry) return lbm_set_err(h, LBM_ESTATE, "lbm_init: call lbm_set_geometry first");
+    if ((rho == nullptr) != (v == nullptr)) return lbm_set_err(h, LBM_EINVAL, "lbm_init: give both rho and v, or neither");
+    cudaSetDevice(h->device);
+    h->cur = 0;
+    h->steps_done = 0;
+    h->macros_valid = false;
+    int rc = LBM_OK;
+    if (h->p.two_phase) {
+        if (!h->have_psi) return lbm_set_err(h, LBM_ESTATE, "lbm_init: two-phase handle needs lbm_set_psi first");
+        if (rho) return lbm_set_err(h, LBM_EINVAL, "lbm_init: two phase starts from rest (rho, v must be NULL)");
+        rc = tp_launch_init(h);
+    } else {
+        float* d_in = nullptr;
+        if (rho) {
+            // gather the dense fields into node order: rho [np], v [3][np]
+            std::vector<float> hin(4 * h->np, 0.0f);
+            for (int32_t n = 0; n < h->n_fluid; ++n) {
+                const int64_t c = h->cell_of_node[n];
+                hin[n] = rho[c];
+                for (int d = 0; d < 3; ++d) hin[(1 + d) * h->np + n] = v[c * 3 + d];
+            }
+            if (cudaMalloc((void**)&d_in, sizeof(float) * 4 * h->np) != cudaSuccess)
+                return lbm_set_err(h, LBM_ENOMEM, "lbm_init: staging allocation failed");
+            rc = lbm_cuda_check(h, cudaMemcpyAsync(d_in, hin.data(), sizeof(float) * 4 * h->np, cudaMemcpyHostToDevice, h->stream), "copy init fields");
+        }
+        if (!rc) rc = sp_launch_init(h, d_in, d_in ? d_in + h->np : nullptr);
+        if (!rc) rc = lbm_cuda_check(h, cudaStreamSynchronize(h->stream), "lbm_init");
+        if (d_in) cudaFree(d_in);
+    }
+    if (!rc) h->initialized = true;
+    return rc;
+}
+
+int lbm_step_async(LbmHandle* h, int32_t n) {
+    if (!h) return lbm_set_err(h, LBM_EINVAL, "lbm_step: NULL handle");
+    if (!h->initialized) return lbm_set_err(h, LBM_ESTATE, "lbm_step: call lbm_init first");
+    if (n < 0) return lbm_set_err(h, LBM_EINVAL, "lbm_step: negative step count");
+    if (n == 0) return LBM_OK;
+    cudaSetDevice(h->device);
+    int rc = h->p.two_phase ? tp_launch_steps(h, n, true) : sp_launch_steps(h, n, true);
+    if (rc) return rc;
+    h->steps_done += n;
+    h->macros_valid = true;
+    return LBM_OK;
+}
+
+int lbm_synchronize(LbmHandle* h) {
+    if (!h) return lbm_set_err(h, LBM_EINVAL, "lbm_synchronize: NULL handle");
+    return lbm_cuda_check(h, cudaStreamSynchronize(h->stream), "stream synchronize");
+}
+
+int lbm_step(LbmHandle* h, int32_t n) {
+    int rc = lbm_step_async(h, n);
+    if (rc) return rc;
+    return lbm_synchronize(h);
+}
+
+int lbm_get_stream(LbmHandle* h, void** stream) {
+    if (!h || !stream) return lbm_set_err(h, LBM_EINVAL, "lbm_get_stream: NULL argument");
+    *stream = (void*)h->stream;
+    return LBM_OK;
+}
+
+}  // extern "C"
+
+namespace {
+// Copy a node-ordered device array (n components of stride np, FP32 or FP64)
+// into a dense host array with `comps` interleaved components; solid cells get
+// `fill`.
+template <typename O>
+int scatter_dense(LbmHandle* h, const void* dsrc, int comps, O* out, O fill) {
+    const size_t rb = h->f64 ? 8 : 4;
+    std::vector<unsigned char> tmp(rb * comps * h->np);
+    int rc = lbm_cuda_check(h, cudaMemcpyAsync(tmp.data(), dsrc, tmp.size(), cudaMemcpyDeviceToHost, h->stream), "copy out");
+    if (!rc) rc = lbm_cuda_check(h, cudaStreamSynchronize(h->stream), "copy out");
+    if (rc) return rc;
+    for (int64_t c = 0; c < h->ncell * comps; ++c) out[c] = fill;
+    for (int32_t n = 0; n < h->n_fluid; ++n) {
+        const int64_t c = h->cell_of_node[n];
+        for (int d = 0; d < comps; ++d) {
+            const int64_t idx = (int64_t)d * h->np + n;
+            out[c * comps + d] = h->f64 ? (O)((const double*)tmp.data())[idx] : (O)((const float*)tmp.data())[idx];
+        }
+    }
+    return LBM_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int lbm_get_macros(LbmHandle* h, float* rho, float* v) {
+    if (!h) return lbm_set_err(h, LBM_EINVAL, "lbm_get_macros: NULL handle");
+    if (!h->have_geometry) return lbm_set_err(h, LBM_ESTATE, "lbm_get_macros: no geometry");
+    cudaSetDevice(h->device);
+    if (!h->macros_valid) {
+        // before the first step: the initial state rho = 1, v = 0 (init, SP:160-170)
+        if (rho) for (int64_t c = 0; c < h->ncell; ++c) rho[c] = 1.0f;
+        if (v) for (int64_t c = 0; c < 3 * h->ncell; ++c) v[c] = 0.0f;
+        return LBM_OK;
+    }
+    int rc = LBM_OK;
+    if (rho) rc = scatter_dense<float>(h, h->d_rho, 1, rho, 1.0f);
+    if (!rc && v) rc = scatter_dense<float>(h, h->d_v, 3, v, 0.0f);
+    return rc;
+}
+
+int lbm_get_macros_f64(LbmHandle* h, double* rho, double* v) {
+    if (!h) return lbm_set_err(h, LBM_EINVAL, "lbm_get_macros_f64: NULL handle");
+    if (!h->have_geometry) return lbm_set_err(h, LBM_ESTATE, "lbm_get_macros_f64: no geometry");
+    cudaSetDevice(h->device);
+    if (!h->macros_valid) {
+        if (rho) for (int64_t c = 0; c < h->ncell; ++c) rho[c] = 1.0;
+        if (v) for (int64_t c = 0; c < 3 * h->ncell; ++c) v[c] = 0.0;
+        return LBM_OK;
+    }
+    int rc = LBM_OK;
+    if (rho) rc = scatter_dense<double>(h, h->d_rho, 1, rho, 1.0);
+    if (!rc && v) rc = scatter_dense<double>(h, h->d_v, 3, v, 0.0);
+    return rc;
+}
+
+int lbm_get_phase(LbmHandle* h, float* psi, float* rho_r, float* rho_b) {
+    if (!h) return lbm_set_err(h, LBM_EINVAL, "lbm_get_phase: NULL handle");
+    if (!h->p.two_phase) return lbm_set_err(h, LBM_ESTATE, "lbm_get_phase: handle is single phase");
+    if (!h->initialized) return lbm_set_err(h, LBM_ESTATE, "lbm_get_phase: call lbm_init first");
+    cudaSetDevice(h->device);
+    int rc = LBM_OK;
+    if (psi) {
+        rc = lbm_cuda_check(h, cudaMemcpyAsync(psi, h->d_psi_dense, sizeof(float) * h->ncell, cudaMemcpyDeviceToHost, h->stream), "copy psi");
+        if (!rc) rc = lbm_cuda_check(h, cudaStreamSynchronize(h->stream), "copy psi");
+    }
+    if (!rc && rho_r) rc = scatter_dense<float>(h, h->d_rr[h->ccur], 1, rho_r, 0.0f);
+    if (!rc && rho_b) rc = scatter_dense<float>(h, h->d_rb[h->ccur], 1, rho_b, 0.0f);
+    return rc;
+}
+
+int lbm_reductions(LbmHandle* h, LbmStats* out) {
+    if (!h || !out) return lbm_set_err(h, LBM_EINVAL, "lbm_reductions: NULL argument");
+    if (!h->have_geometry) return lbm_set_err(h, LBM_ESTATE, "lbm_reductions: no geometry");
+    cudaSetDevice(h->device);
+    if (!h->macros_valid) {
+        out->mass = (double)h->n_fluid;
+        out->mom[0] = out->mom[1] = out->mom[2] = 0;
+        out->max_v = 0;
+        out->n_nonfinite = 0;
+        out->n_fluid = h->n_fluid;
+        return LBM_OK;
+    }
+    return red_launch(h, out, nullptr);
+}
+
+int lbm_get_max_v(LbmHandle* h, float* out) {
+    if (!h || !out) return lbm_set_err(h, LBM_EINVAL, "lbm_get_max_v: NULL argument");
+    if (!h->have_geometry) return lbm_set_err(h, LBM_ESTATE, "lbm_get_max_v: no geometry");
+    if (!h->macros_valid) { *out = 0.0f; return LBM_OK; }
+    cudaSetDevice(h->device);
+    LbmStats st;
+    return red_launch(h, &st, out);
+}
+
+int lbm_get_info(LbmHandle* h, LbmInfo* out) {
+    if (!h || !out) return lbm_set_err(h, LBM_EINVAL, "lbm_get_info: NULL argument");
+    out->n_cells = h->ncell;
+    out->n_fluid = h->n_fluid;
+    out->steps_done = h->steps_done;
+    out->device_bytes = h->device_bytes;
+    out->storage = h->p.storage;
+    out->two_phase = h->p.two_phase;
+    out->sm_count = h->sm_count;
+    out->abi_version = LBM_ABI_VERSION;
+    return LBM_OK;
+}
+
+int lbm_get_fluid_index(LbmHandle* h, int32_t* cell_of_node) {
+    if (!h || !cell_of_node) return lbm_set_err(h, LBM_EINVAL, "lbm_get_fluid_index: NULL argument");
+    if (!h->have_geometry) return lbm_set_err(h, LBM_ESTATE, "lbm_get_fluid_index: no geometry");
+    std::memcpy(cell_of_node, h->cell_of_node.data(), sizeof(int32_t) * h->n_fluid);
+    return LBM_OK;
+}
+
+int lbm_get_neighbors(LbmHandle* h, int32_t* src) {
+    if (!h || !src) return lbm_set_err(h, LBM_EINVAL, "lbm_get_neighbors: NULL argument");
+    if (!h->have_geometry) return lbm_set_err(h, LBM_ESTATE, "lbm_get_neighbors: no geometry");
+    // Read the map back from the device: the table is what the kernels use.
+    std::vector<int32_t> map(h->ncell);
+    int rc = lbm_cuda_check(h, cudaMemcpy(map.data(), h->d_map, sizeof(int32_t) * h->ncell, cudaMemcpyDeviceToHost), "copy map");
+    if (rc) return rc;
+    const int nx = h->p.nx, ny = h->p.ny, nz = h->p.nz;
+    for (int32_t n = 0; n < h->n_fluid; ++n) {
+        const int64_t c = h->cell_of_node[n];
+        const int i = (int)(c % nx), j = (int)((c / nx) % ny), k = (int)(c / ((int64_t)nx * ny));
+        for (int s = 1; s < 19; ++s) {
+            int x = i - lbm_ex(s), y = j - lbm_ey(s), z = k - lbm_ez(s);
+            if (x < 0) x = nx - 1;
+            if (x > nx - 1) x = 0;
+            if (y < 0) y = ny - 1;
+            if (y > ny - 1) y = 0;
+            if (z < 0) z = nz - 1;
+            if (z > nz - 1) z = 0;
+            const int32_t m = map[x + (int64_t)nx * (y + (int64_t)ny * z)];
+            src[(int64_t)(s - 1) * h->n_fluid + n] = m >= 0 ? m : -1 - n;
+        }
+    }
+    return LBM_OK;
+}
+
+int lbm_get_populations(LbmHandle* h, double* f) {
+    if (!h || !f) return lbm_set_err(h, LBM_EINVAL, "lbm_get_populations: NULL argument");
+    if (!h->initialized || h->p.two_phase) return lbm_set_err(h, LBM_ESTATE, "lbm_get_populations: needs an initialised single-phase handle");
+    std::vector<unsigned char> tmp(h->elem * 19 * h->np);
+    int rc = lbm_cuda_check(h, cudaMemcpy(tmp.data(), h->d_f[h->cur], tmp.size(), cudaMemcpyDeviceToHost), "copy f");
+    if (rc) return rc;
+    for (int s = 0; s < 19; ++s)
+        for (int32_t n = 0; n < h->n_fluid; ++n) {
+            const int64_t idx = (int64_t)s * h->np + n;
+            double val = 0;
+            switch (h->p.storage) {
+            case LBM_STORE_F32: val = ((const float*)tmp.data())[idx]; break;
+            case LBM_STORE_F64: val = ((const double*)tmp.data())[idx]; break;
+            case LBM_STORE_F16_DEV: val = lbm_w(s) + (double)__half2float(((const __half*)tmp.data())[idx]) / 4096.0; break;
+            case LBM_STORE_BF16_DEV: val = lbm_w(s) + (double)__bfloat162float(((const __nv_bfloat16*)tmp.data())[idx]); break;
+            }
+            f[(int64_t)s * h->n_fluid + n] = val;
+        }
+    return LBM_OK;
+}
+
+int lbm_set_populations(LbmHandle* h, const double* f) {
+    if (!h || !f) return lbm_set_err(h, LBM_EINVAL, "lbm_set_populations: NULL argument");
+    if (!h->initialized || h->p.two_phase) return lbm_set_err(h, LBM_ESTATE, "lbm_set_populations: needs an initialised single-phase handle");
+    std::vector<unsigned char> tmp(h->elem * 19 * h->np, 0);
+    for (int s = 0; s < 19; ++s)
+        for (int32_t n = 0; n < h->n_fluid; ++n) {
+            const int64_t idx = (int64_t)s * h->np + n;
+            const double val = f[(int64_t)s * h->n_fluid + n];
+            switch (h->p.storage) {
+            case LBM_STORE_F32: ((float*)tmp.data())[idx] = (float)val; break;
+            case LBM_STORE_F64: ((double*)tmp.data())[idx] = val; break;
+            case LBM_STORE_F16_DEV: ((__half*)tmp.data())[idx] = __float2half_rn((float)((val - lbm_w(s)) * 4096.0)); break;
+            case LBM_STORE_BF16_DEV: ((__nv_bfloat16*)tmp.data())[idx] = __float2bfloat16_rn((float)(val - lbm_w(s))); break;
+            }
+        }
+    int rc = lbm_cuda_check(h, cudaMemcpy(h->d_f[h->cur], tmp.data(), tmp.size(), cudaMemcpyHostToDevice), "copy f");
+    h->macros_valid = false;
+    return rc;
+}
+
+int lbm_debug_stream(LbmHandle* h, const float* f_in, float* f_out) {
+    if (!h || !f_in || !f_out) return lbm_set_err(h, LBM_EINVAL, "lbm_debug_stream: NULL argument");
+    if (!h->have_geometry) return lbm_set_err(h, LBM_ESTATE, "lbm_debug_stream: no geometry");
+    cudaSetDevice(h->device);
+    float *din = nullptr, *dout = nullptr;
+    const size_t bytes = sizeof(float) * 19 * h->np;
+    if (cudaMalloc((void**)&din, bytes) != cudaSuccess || cudaMalloc((void**)&dout, bytes) != cudaSuccess) {
+        if (din) cudaFree(din);
+        return lbm_set_err(h, LBM_ENOMEM, "lbm_debug_stream: allocation failed");
+    }
+    std::vector<float> tmp(19 * h->np, 0.0f);
+    for (int s = 0; s < 19; ++s)
+        for (int32_t n = 0; n < h->n_fluid; ++n) tmp[(int64_t)s * h->np + n] = f_in[(int64_t)s * h->n_fluid + n];
+    int rc = lbm_cuda_check(h, cudaMemcpy(din, tmp.data(), bytes, cudaMemcpyHostToDevice), "copy in");
+    if (!rc) rc = sp_launch_debug_stream(h, din, dout);
+    if (!rc) rc = lbm_cuda_check(h, cudaStreamSynchronize(h->stream), "debug stream");
+    if (!rc) rc = lbm_cuda_check(h, cudaMemcpy(tmp.data(), dout, bytes, cudaMemcpyDeviceToHost), "copy out");
+    if (!rc)
+        for (int s = 0; s < 19; ++s)
+            for (int32_t n = 0; n < h->n_fluid; ++n) f_out[(int64_t)s * h->n_fluid + n] = tmp[(int64_t)s * h->np + n];
+    cudaFree(din);
+    cudaFree(dout);
+    return rc;
+}
+
+int lbm_last_error(LbmHandle* h, char* buf, size_t n) {
+    if (!buf || n == 0) return LBM_EINVAL;
+    std::string m;
+    if (h) m = h->err;
+    else {
+        std::lock_guard<std::mutex> lk(g_err_mu);
+        m = g_err;
+    }
+    std::snprintf(buf, n, "%s", m.c_str());
+    return LBM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,142 @@
+// D3Q19 tables, equilibrium and population storage codecs shared by the
+// fused kernels.  Arithmetic is written term by term in the order of the
+// reference's Taichi expressions (paths inside the taichi_LBM3D tree):
+//   SP = Single_phase/LBM_3D_SinglePhase_Solver.py
+//   TP = 2phase/lbm_solver_3d_2phase_sparse.py
+// and the library is compiled with -fmad=false, so that no multiply-add is
+// fused unless written as lbm_fma() on an exact product.  Together with IEEE
+// division this makes the FP32 kernels reproduce the reference arithmetic
+// bit for bit (terms with an exactly-zero coefficient are dropped, which does
+// not change a non-zero partial sum).
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+#include "../../include/lbm_gb300.h"
+
+#define LBM_HD __host__ __device__ __forceinline__
+
+// e, w, LR: SP:183-197, SP:85.
+__host__ __device__ constexpr int lbm_ex(int s) {
+    return (s == 1 || s == 7 || s == 9 || s == 11 || s == 13) ? 1
+         : (s == 2 || s == 8 || s == 10 || s == 12 || s == 14) ? -1 : 0;
+}
+__host__ __device__ constexpr int lbm_ey(int s) {
+    return (s == 3 || s == 7 || s == 10 || s == 15 || s == 17) ? 1
+         : (s == 4 || s == 8 || s == 9 || s == 16 || s == 18) ? -1 : 0;
+}
+__host__ __device__ constexpr int lbm_ez(int s) {
+    return (s == 5 || s == 11 || s == 14 || s == 15 || s == 18) ? 1
+         : (s == 6 || s == 12 || s == 13 || s == 16 || s == 17) ? -1 : 0;
+}
+__host__ __device__ constexpr int lbm_lr(int s) { return s == 0 ? 0 : ((s & 1) ? s + 1 : s - 1); }
+__host__ __device__ constexpr double lbm_w(int s) { return s == 0 ? 1.0 / 3.0 : (s <= 6 ? 1.0 / 18.0 : 1.0 / 36.0); }
+// S_dig pattern (SP:131): 0 conserved, 1 s_v, 2 s_other.
+__host__ __device__ constexpr int lbm_skind(int s) {
+    return (s == 0 || s == 3 || s == 5 || s == 7) ? 0 : ((s == 4 || s == 6 || s == 8 || s >= 16) ? 2 : 1);
+}
+
+template <typename R>
+LBM_HD R lbm_fma(R a, R b, R c);
+template <>
+LBM_HD float lbm_fma<float>(float a, float b, float c) {
+#ifdef __CUDA_ARCH__
+    return __fmaf_rn(a, b, c);
+#else
+    return fmaf(a, b, c);
+#endif
+}
+template <>
+LBM_HD double lbm_fma<double>(double a, double b, double c) {
+#ifdef __CUDA_ARCH__
+    return __fma_rn(a, b, c);
+#else
+    return fma(a, b, c);
+#endif
+}
+
+#include "mrt_gen.cuh"
+
+// e_s . u with the zero components dropped (SP:154 e[k].dot(u)).
+template <int S, typename R>
+LBM_HD R lbm_edot(R u0, R u1, R u2) {
+    constexpr int ex = lbm_ex(S), ey = lbm_ey(S), ez = lbm_ez(S);
+    if constexpr (ex == 0 && ey == 0 && ez == 0) {
+        return (R)0;
+    } else if constexpr (ex != 0) {
+        R a = ex > 0 ? u0 : -u0;
+        if constexpr (ey != 0) a = ey > 0 ? a + u1 : a - u1;
+        if constexpr (ez != 0) a = ez > 0 ? a + u2 : a - u2;
+        return a;
+    } else if constexpr (ey != 0) {
+        R a = ey > 0 ? u1 : -u1;
+        if constexpr (ez != 0) a = ez > 0 ? a + u2 : a - u2;
+        return a;
+    } else {
+        return ez > 0 ? u2 : -u2;
+    }
+}
+
+// feq (SP:152-158): w*rho*(1.0+3.0*eu+4.5*eu*eu-1.5*uv), uv = u.u precomputed.
+template <int S, typename R>
+LBM_HD R lbm_feq(R rho, R u0, R u1, R u2, R uv) {
+    R eu = lbm_edot<S, R>(u0, u1, u2);
+    R t = (R)1.0 + (R)3.0 * eu;
+    t = t + ((R)4.5 * eu) * eu;
+    t = t - (R)1.5 * uv;
+    return ((R)lbm_w(S) * rho) * t;
+}
+
+template <typename R>
+LBM_HD R lbm_usq(R u0, R u1, R u2) {
+    R a = u0 * u0;
+    a = a + u1 * u1;
+    return a + u2 * u2;
+}
+
+// Runtime-direction feq (face boundary conditions).
+template <typename R>
+__device__ __forceinline__ void lbm_feq_all(R rho, R u0, R u1, R u2, R* out) {
+    const R uv = lbm_usq(u0, u1, u2);
+#define LBM_FQ(S) out[S] = lbm_feq<S, R>(rho, u0, u1, u2, uv);
+    LBM_FQ(0) LBM_FQ(1) LBM_FQ(2) LBM_FQ(3) LBM_FQ(4) LBM_FQ(5) LBM_FQ(6) LBM_FQ(7) LBM_FQ(8) LBM_FQ(9)
+    LBM_FQ(10) LBM_FQ(11) LBM_FQ(12) LBM_FQ(13) LBM_FQ(14) LBM_FQ(15) LBM_FQ(16) LBM_FQ(17) LBM_FQ(18)
+#undef LBM_FQ
+}
+
+// ---------------------------------------------------------------- storage
+// Population codecs: Codec<STORE>::T is the stored element type; R the compute
+// type.  Deviation storage keeps f_s - w_s (rho0 = 1), scaled by 2^12 in FP16
+// so that deviations down to ~1e-8 stay in FP16's normal range.
+template <int STORE> struct Codec;
+template <> struct Codec<LBM_STORE_F32> {
+    using T = float; using R = float;
+    template <int S> static __device__ __forceinline__ R dec(T x) { return x; }
+    template <int S> static __device__ __forceinline__ T enc(R f) { return f; }
+};
+template <> struct Codec<LBM_STORE_F64> {
+    using T = double; using R = double;
+    template <int S> static __device__ __forceinline__ R dec(T x) { return x; }
+    template <int S> static __device__ __forceinline__ T enc(R f) { return f; }
+};
+template <> struct Codec<LBM_STORE_F16_DEV> {
+    using T = __half; using R = float;
+    template <int S> static __device__ __forceinline__ R dec(T x) {
+        return __fmaf_rn(__half2float(x), 1.0f / 4096.0f, (float)lbm_w(S));
+    }
+    template <int S> static __device__ __forceinline__ T enc(R f) {
+        return __float2half_rn((f - (float)lbm_w(S)) * 4096.0f);
+    }
+};
+template <> struct Codec<LBM_STORE_BF16_DEV> {
+    using T = __nv_bfloat16; using R = float;
+    template <int S> static __device__ __forceinline__ R dec(T x) { return __bfloat162float(x) + (float)lbm_w(S); }
+    template <int S> static __device__ __forceinline__ T enc(R f) { return __float2bfloat16_rn(f - (float)lbm_w(S)); }
+};
+
+// Lattice coordinates of a fluid node, packed i | j<<11 | k<<22.
+LBM_HD uint32_t lbm_pack(int i, int j, int k) { return (uint32_t)i | ((uint32_t)j << 11) | ((uint32_t)k << 22); }
+LBM_HD int lbm_pi(uint32_t p) { return (int)(p & 2047u); }
+LBM_HD int lbm_pj(uint32_t p) { return (int)((p >> 11) & 2047u); }
+LBM_HD int lbm_pk(uint32_t p) { return (int)(p >> 22); }

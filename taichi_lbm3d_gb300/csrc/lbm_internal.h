@@ -1,0 +1,85 @@
+// Internal state of an LbmHandle and the launchers the C ABI calls.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/lbm_gb300.h"
+
+// Per-launch constants of the single-phase step (template on compute type R).
+template <typename R>
+struct SpConsts {
+    int32_t nx, ny, nz;
+    int32_t n_fluid;
+    int64_t np;        // element stride between populations (padded n_fluid)
+    int32_t bc[6];
+    int32_t bc_form;
+    int32_t any_bc;
+    int32_t any_pressure;
+    int32_t guo;
+    R rho_bc[6];
+    R vel_bc[6][3];
+    R sv, so;          // S_dig values s_v, s_other (SP:128-131)
+    R fext[3];
+    R fhalf[3];        // fext / 2 (SP:388)
+};
+
+struct LbmHandle {
+    LbmParams p{};
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    int64_t ncell = 0;
+    int32_t n_fluid = 0;
+    int64_t np = 0;
+    bool have_geometry = false, initialized = false, macros_valid = false, have_psi = false;
+    int64_t steps_done = 0;
+    int32_t block = 256;
+    size_t elem = 4;          // bytes per stored population
+    bool f64 = false;         // compute in FP64
+    bool force = false;
+
+    std::vector<int8_t> solid;             // dense host copy
+    std::vector<int32_t> cell_of_node;     // n_fluid
+    std::vector<float> psi0;               // dense initial psi (two phase)
+
+    int32_t* d_map = nullptr;              // dense: node index or -1 (solid)
+    uint32_t* d_coord = nullptr;           // packed (i,j,k) per node
+    void* d_f[2] = {nullptr, nullptr};     // populations [19][np]
+    int cur = 0;
+    void* d_vprev = nullptr;               // [3][np] previous-step v (pressure faces)
+    void* d_rho = nullptr;                 // [np]
+    void* d_v = nullptr;                   // [3][np]
+    // two phase
+    void* d_psi = nullptr;                 // [np] psi at fluid nodes
+    void* d_rr[2] = {nullptr, nullptr};    // rho_r, double-buffered [np]
+    void* d_rb[2] = {nullptr, nullptr};    // rho_b
+    void* d_cg = nullptr;                  // colour gradient C [3][np]
+    float* d_psi_dense = nullptr;          // dense psi of every cell (solid cells keep input)
+    int ccur = 0;
+    // reductions
+    double* d_red = nullptr;               // per-block partials
+    int red_blocks = 0;
+    double* d_red_out = nullptr;
+    int64_t device_bytes = 0;
+    std::string err;
+};
+
+int lbm_set_err(LbmHandle* h, int code, const std::string& msg);
+int lbm_cuda_check(LbmHandle* h, cudaError_t e, const char* what);
+
+// single phase (lbm_sp.cu)
+int sp_launch_init(LbmHandle* h, const void* rho_nodes, const void* v_nodes);
+int sp_launch_steps(LbmHandle* h, int32_t n, bool macros_last);
+int sp_launch_debug_stream(LbmHandle* h, const float* d_in, float* d_out);
+template <typename R>
+SpConsts<R> sp_make_consts(const LbmHandle* h);
+
+// two phase (lbm_tp.cu)
+int tp_launch_init(LbmHandle* h);
+int tp_launch_steps(LbmHandle* h, int32_t n, bool macros_last);
+
+// reductions (lbm_reduce.cu)
+int red_launch(LbmHandle* h, LbmStats* out, float* max_v_f32);
