@@ -167,6 +167,22 @@ int lbm_debug_stream(LbmHandle* h, const float* f_in, float* f_out);
  * when h is NULL) into buf. */
 int lbm_last_error(LbmHandle* h, char* buf, size_t n);
 
+/* No counterpart in the reference.  The FP64 reduction of lbm_reductions for
+ * callers that cannot allocate device memory: a host framework whose own pool
+ * allocator already owns the GPU's memory, or a time-critical loop that must not
+ * risk the device-wide synchronisation of cudaMalloc / cudaFree.  The caller
+ * passes device arrays in node order (rho[n], v[3][v_stride], FP32), a stream
+ * (NULL = default stream) and a host LbmStats; the call allocates nothing.  Its
+ * scratch is a static device array of LBM_NOALLOC_SCRATCH_BYTES that every GPU
+ * loading the library holds until exit.  n above LBM_NOALLOC_MAX_NODES is
+ * rejected with LBM_EINVAL.  The first call on a device looks up the scratch's
+ * device address (make it before any stream capture).  Calls share the scratch:
+ * calls that overlap on the GPU race and must be serialised by the caller. */
+#define LBM_NOALLOC_MAX_NODES 67108864
+#define LBM_NOALLOC_SCRATCH_BYTES 196656
+int lbm_reduce_macros_noalloc(const float* rho, const float* v, int64_t n, int64_t v_stride, void* stream,
+                              LbmStats* out);
+
 #ifdef __cplusplus
 }
 #endif
