@@ -53,16 +53,25 @@ def _compile(src, verbose=False):
     obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
     if not _stale(obj, [src] + _headers()):
         return obj, ""
-    cmd = [_nvcc()] + NVCC_FLAGS + ["-Xptxas", "-v", "-c", src, "-o", obj]
+    cmd = [_nvcc()] + NVCC_FLAGS + _extra_flags() + ["-Xptxas", "-v", "-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (src, " ".join(cmd), r.stderr[-4000:]))
     return obj, r.stderr
 
 
+def _extra_flags():
+    """Extra nvcc flags from LBM_NVCC_EXTRA (e.g. "-DLBM_SP_MINBLOCKS=6") for tuning builds."""
+    return os.environ.get("LBM_NVCC_EXTRA", "").split()
+
+
 def build(force=False, verbose=False):
     os.makedirs(BUILD, exist_ok=True)
     srcs = sources()
+    stamp = os.path.join(BUILD, "flags.txt")
+    flags = " ".join(NVCC_FLAGS + _extra_flags())
+    if not os.path.exists(stamp) or open(stamp).read() != flags:
+        force = True
     if force:
         for f in os.listdir(BUILD):
             os.remove(os.path.join(BUILD, f))
@@ -80,6 +89,8 @@ def build(force=False, verbose=False):
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s" % r.stderr[-4000:])
         os.replace(tmp, LIB)
+    with open(stamp, "w") as fh:
+        fh.write(flags)
     return LIB
 
 

@@ -464,7 +464,7 @@ int lbm_get_populations(LbmHandle* h, double* f) {
     if (rc) return rc;
     for (int s = 0; s < 19; ++s)
         for (int32_t n = 0; n < h->n_fluid; ++n) {
-            const int64_t idx = (int64_t)s * h->np + n;
+            const int64_t idx = lbm_pidx(n, s);
             double val = 0;
             switch (h->p.storage) {
             case LBM_STORE_F32: val = ((const float*)tmp.data())[idx]; break;
@@ -483,7 +483,7 @@ int lbm_set_populations(LbmHandle* h, const double* f) {
     std::vector<unsigned char> tmp(h->elem * 19 * h->np, 0);
     for (int s = 0; s < 19; ++s)
         for (int32_t n = 0; n < h->n_fluid; ++n) {
-            const int64_t idx = (int64_t)s * h->np + n;
+            const int64_t idx = lbm_pidx(n, s);
             const double val = f[(int64_t)s * h->n_fluid + n];
             switch (h->p.storage) {
             case LBM_STORE_F32: ((float*)tmp.data())[idx] = (float)val; break;
@@ -509,14 +509,14 @@ int lbm_debug_stream(LbmHandle* h, const float* f_in, float* f_out) {
     }
     std::vector<float> tmp(19 * h->np, 0.0f);
     for (int s = 0; s < 19; ++s)
-        for (int32_t n = 0; n < h->n_fluid; ++n) tmp[(int64_t)s * h->np + n] = f_in[(int64_t)s * h->n_fluid + n];
+        for (int32_t n = 0; n < h->n_fluid; ++n) tmp[lbm_pidx(n, s)] = f_in[(int64_t)s * h->n_fluid + n];
     int rc = lbm_cuda_check(h, cudaMemcpy(din, tmp.data(), bytes, cudaMemcpyHostToDevice), "copy in");
     if (!rc) rc = sp_launch_debug_stream(h, din, dout);
     if (!rc) rc = lbm_cuda_check(h, cudaStreamSynchronize(h->stream), "debug stream");
     if (!rc) rc = lbm_cuda_check(h, cudaMemcpy(tmp.data(), dout, bytes, cudaMemcpyDeviceToHost), "copy out");
     if (!rc)
         for (int s = 0; s < 19; ++s)
-            for (int32_t n = 0; n < h->n_fluid; ++n) f_out[(int64_t)s * h->n_fluid + n] = tmp[(int64_t)s * h->np + n];
+            for (int32_t n = 0; n < h->n_fluid; ++n) f_out[(int64_t)s * h->n_fluid + n] = tmp[lbm_pidx(n, s)];
     cudaFree(din);
     cudaFree(dout);
     return rc;

@@ -135,6 +135,14 @@ template <> struct Codec<LBM_STORE_BF16_DEV> {
     template <int S> static __device__ __forceinline__ T enc(R f) { return __float2bfloat16_rn(f - (float)lbm_w(S)); }
 };
 
+// Population layout "AoSoA-32": nodes in chunks of 32; within a chunk the 19
+// directions follow one another, 32 consecutive nodes each.  Element (n, s) is
+// at lbm_eoff(n) + 32*s, so a warp's 32 nodes touch one 128 B (FP32) segment per
+// direction and a thread addresses all 19 of its slots with immediate offsets.
+LBM_HD int64_t lbm_eoff(int64_t n) { return n + (n >> 5) * 576; }
+LBM_HD int64_t lbm_pidx(int64_t n, int s) { return lbm_eoff(n) + 32 * s; }
+__device__ __forceinline__ int lbm_eoff32(int n) { return n + (n >> 5) * 576; }
+
 // Lattice coordinates of a fluid node, packed i | j<<11 | k<<22.
 LBM_HD uint32_t lbm_pack(int i, int j, int k) { return (uint32_t)i | ((uint32_t)j << 11) | ((uint32_t)k << 22); }
 LBM_HD int lbm_pi(uint32_t p) { return (int)(p & 2047u); }

@@ -20,34 +20,82 @@
 #include "lbm_common.cuh"
 #include "lbm_internal.h"
 
+// Resident CTAs per SM requested for the unforced FP32/16-bit step kernel
+// (caps registers at 65536 / (256 * LBM_SP_MINBLOCKS)).
+#ifndef LBM_SP_MINBLOCKS
+#define LBM_SP_MINBLOCKS 6
+#endif
+
 namespace {
 
-// Source cell of the pull for direction S: x - e_S with periodic wrap.
-template <int S>
-__device__ __forceinline__ int src_cell(int nx, int ny, int i, int j, int k, int xm, int xp, int ym, int yp, int zm,
-                                        int zp) {
-    constexpr int ex = lbm_ex(S), ey = lbm_ey(S), ez = lbm_ez(S);
-    const int x = ex > 0 ? xm : (ex < 0 ? xp : i);
-    const int y = ey > 0 ? ym : (ey < 0 ? yp : j);
-    const int z = ez > 0 ? zm : (ez < 0 ? zp : k);
-    return x + nx * (y + ny * z);
+// Pull sources.  For node x and direction S the population comes from the
+// node at x - e_S (periodic wrap, SP:247-257), or -- when that cell is solid --
+// from the node's own LR[S] slot (halfway bounce-back, SP:265-268).  The cell is
+// looked up in the dense map through 9 row offsets (one per (y, z) pair); when
+// no lane of the warp sits on an x face the x neighbours are at +-1 from the
+// row offset, so each lookup is one load with an immediate offset.
+struct Rows {
+    int r[3][3];  // [source y: j-1, j, j+1 wrapped][source z], cell index of (i, y, z)
+};
+
+__device__ __forceinline__ Rows make_rows(int nx, int ny, int i, int j, int k, int ym, int yp, int zm, int zp) {
+    Rows R;
+    const int ys[3] = {ym, j, yp};
+    const int zs[3] = {zm, k, zp};
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) R.r[a][b] = i + nx * (ys[a] + ny * zs[b]);
+    return R;
 }
 
-template <int STORE>
+template <int STORE, bool XWRAP>
 struct Gather {
     using Cd = Codec<STORE>;
     using T = typename Cd::T;
     using R = typename Cd::R;
     template <int S>
-    static __device__ __forceinline__ void one(R* F, const T* __restrict__ fin, const int32_t* __restrict__ map,
-                                               int64_t np, int n, int nx, int ny, int i, int j, int k, int xm, int xp,
-                                               int ym, int yp, int zm, int zp) {
-        const int cell = src_cell<S>(nx, ny, i, j, k, xm, xp, ym, yp, zm, zp);
-        const int src = __ldg(map + cell);
-        const T* p = src >= 0 ? fin + (int64_t)S * np + src : fin + (int64_t)lbm_lr(S) * np + n;
-        F[S] = Cd::template dec<S>(*p);
+    static __device__ __forceinline__ void one(R* F, const T* __restrict__ fin, const T* __restrict__ own,
+                                               const int32_t* __restrict__ map, const Rows& rows, int i, int xm,
+                                               int xp) {
+        constexpr int ex = lbm_ex(S), ey = lbm_ey(S), ez = lbm_ez(S);
+        // source is x - e_S: row index 0 holds y-1 (used when ey = +1)
+        const int row = rows.r[1 - ey][1 - ez];
+        int src;
+        if constexpr (XWRAP) {
+            const int x = ex > 0 ? xm : (ex < 0 ? xp : i);
+            src = __ldg(map + (row - i + x));
+        } else {
+            src = __ldg(map + row - ex);
+        }
+        if (src >= 0) F[S] = Cd::template dec<S>(fin[lbm_eoff32(src) + 32 * S]);
+        else F[S] = Cd::template dec<S>(own[32 * lbm_lr(S)]);
+    }
+    static __device__ __forceinline__ void all(R* F, const T* __restrict__ fin, const T* __restrict__ own,
+                                               const int32_t* __restrict__ map, const Rows& rows, int i, int xm,
+                                               int xp) {
+        F[0] = Cd::template dec<0>(own[0]);
+#define LBM_G(S) one<S>(F, fin, own, map, rows, i, xm, xp);
+        LBM_G(1) LBM_G(2) LBM_G(3) LBM_G(4) LBM_G(5) LBM_G(6) LBM_G(7) LBM_G(8) LBM_G(9)
+        LBM_G(10) LBM_G(11) LBM_G(12) LBM_G(13) LBM_G(14) LBM_G(15) LBM_G(16) LBM_G(17) LBM_G(18)
+#undef LBM_G
     }
 };
+
+// Gather F for node n; warps with no lane on an x face take the immediate-offset path.
+template <int STORE>
+__device__ __forceinline__ void gather_node(typename Codec<STORE>::R* F, const typename Codec<STORE>::T* __restrict__ fin,
+                                            const int32_t* __restrict__ map, int n, int nx, int ny, int nz, int i, int j,
+                                            int k) {
+    const int xm = i == 0 ? nx - 1 : i - 1, xp = i == nx - 1 ? 0 : i + 1;
+    const int ym = j == 0 ? ny - 1 : j - 1, yp = j == ny - 1 ? 0 : j + 1;
+    const int zm = k == 0 ? nz - 1 : k - 1, zp = k == nz - 1 ? 0 : k + 1;
+    const Rows rows = make_rows(nx, ny, i, j, k, ym, yp, zm, zp);
+    const typename Codec<STORE>::T* own = fin + lbm_eoff32(n);
+    const bool x_inside = i > 0 && i < nx - 1;
+    if (__all_sync(__activemask(), x_inside)) Gather<STORE, false>::all(F, fin, own, map, rows, i, xm, xp);
+    else Gather<STORE, true>::all(F, fin, own, map, rows, i, xm, xp);
+}
 
 #define LBM_ALL_DIRS(X) X(1) X(2) X(3) X(4) X(5) X(6) X(7) X(8) X(9) X(10) X(11) X(12) X(13) X(14) X(15) X(16) X(17) X(18)
 
@@ -169,7 +217,7 @@ __device__ __forceinline__ bool on_face(int i, int j, int k, const SpConsts<R>& 
 }
 
 template <int STORE, bool FORCE, bool MACROS>
-__global__ void __launch_bounds__(256) sp_step_kernel(const __grid_constant__ SpConsts<typename Codec<STORE>::R> C,
+__global__ void __launch_bounds__(256, STORE == LBM_STORE_F64 ? 1 : (FORCE ? 4 : LBM_SP_MINBLOCKS)) sp_step_kernel(const __grid_constant__ SpConsts<typename Codec<STORE>::R> C,
                                                       const typename Codec<STORE>::T* __restrict__ fin,
                                                       typename Codec<STORE>::T* __restrict__ fout,
                                                       const int32_t* __restrict__ map,
@@ -183,17 +231,10 @@ __global__ void __launch_bounds__(256) sp_step_kernel(const __grid_constant__ Sp
     if (n >= C.n_fluid) return;
     const uint32_t pc = __ldg(coord + n);
     const int i = lbm_pi(pc), j = lbm_pj(pc), k = lbm_pk(pc);
-    const int nx = C.nx, ny = C.ny;
-    const int xm = i == 0 ? nx - 1 : i - 1, xp = i == nx - 1 ? 0 : i + 1;
-    const int ym = j == 0 ? ny - 1 : j - 1, yp = j == ny - 1 ? 0 : j + 1;
-    const int zm = k == 0 ? C.nz - 1 : k - 1, zp = k == C.nz - 1 ? 0 : k + 1;
     const int64_t np = C.np;
 
     R F[19];
-    F[0] = Cd::template dec<0>(fin[n]);
-#define LBM_G(S) Gather<STORE>::template one<S>(F, fin, map, np, n, nx, ny, i, j, k, xm, xp, ym, yp, zm, zp);
-    LBM_ALL_DIRS(LBM_G)
-#undef LBM_G
+    gather_node<STORE>(F, fin, map, n, C.nx, C.ny, C.nz, i, j, k);
 
     // Face nodes are rare; warps without one skip the branch uniformly.
     bool face = false;
@@ -228,7 +269,8 @@ __global__ void __launch_bounds__(256) sp_step_kernel(const __grid_constant__ Sp
     }
 
     collide_sp<R, FORCE>(F, r, vx, vy, vz, C);
-#define LBM_S(S) fout[(int64_t)S * np + n] = Cd::template enc<S>(F[S]);
+    typename Cd::T* out = fout + lbm_eoff32(n);
+#define LBM_S(S) out[32 * S] = Cd::template enc<S>(F[S]);
     LBM_S(0) LBM_ALL_DIRS(LBM_S)
 #undef LBM_S
 }
@@ -257,7 +299,8 @@ __global__ void sp_init_kernel(const __grid_constant__ SpConsts<typename Codec<S
     vprev[np + n] = vy;
     vprev[2 * np + n] = vz;
     collide_sp<R, FORCE>(F, r, vx, vy, vz, C);
-#define LBM_S(S) fout[(int64_t)S * np + n] = Cd::template enc<S>(F[S]);
+    typename Cd::T* out = fout + lbm_eoff32(n);
+#define LBM_S(S) out[32 * S] = Cd::template enc<S>(F[S]);
     LBM_S(0) LBM_ALL_DIRS(LBM_S)
 #undef LBM_S
 }
@@ -269,18 +312,11 @@ __global__ void sp_gather_kernel(const __grid_constant__ SpConsts<float> C, cons
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= C.n_fluid) return;
     const uint32_t pc = coord[n];
-    const int i = lbm_pi(pc), j = lbm_pj(pc), k = lbm_pk(pc);
-    const int nx = C.nx, ny = C.ny;
-    const int xm = i == 0 ? nx - 1 : i - 1, xp = i == nx - 1 ? 0 : i + 1;
-    const int ym = j == 0 ? ny - 1 : j - 1, yp = j == ny - 1 ? 0 : j + 1;
-    const int zm = k == 0 ? C.nz - 1 : k - 1, zp = k == C.nz - 1 ? 0 : k + 1;
     float F[19];
-    F[0] = fin[n];
-#define LBM_G(S) Gather<LBM_STORE_F32>::template one<S>(F, fin, map, C.np, n, nx, ny, i, j, k, xm, xp, ym, yp, zm, zp);
-    LBM_ALL_DIRS(LBM_G)
-#undef LBM_G
+    gather_node<LBM_STORE_F32>(F, fin, map, n, C.nx, C.ny, C.nz, lbm_pi(pc), lbm_pj(pc), lbm_pk(pc));
+    float* out = fout + lbm_eoff32(n);
 #pragma unroll
-    for (int s = 0; s < 19; ++s) fout[(int64_t)s * C.np + n] = F[s];
+    for (int s = 0; s < 19; ++s) out[32 * s] = F[s];
 }
 
 template <int STORE, bool FORCE, bool MACROS>
