@@ -11,5 +11,6 @@ All compute runs in liblbm_gb300.so (hand-written CUDA for sm_103a, called
 through ctypes); there is no CPU fallback.
 """
 from .solver import LB3D_Solver_Single_Phase  # noqa: F401
+from .two_phase import LB3D_Solver_Two_Phase  # noqa: F401
 
-__all__ = ["LB3D_Solver_Single_Phase"]
+__all__ = ["LB3D_Solver_Single_Phase", "LB3D_Solver_Two_Phase"]

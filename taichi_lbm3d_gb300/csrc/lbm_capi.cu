@@ -55,8 +55,7 @@ void free_lattice(LbmHandle* h) {
     dev_free(h->d_rr[1]);
     dev_free(h->d_rb[0]);
     dev_free(h->d_rb[1]);
-    dev_free(h->d_cg);
-    dev_free(h->d_psi_dense);
+    dev_free(h->d_cs);
     dev_free(h->d_red);
     dev_free(h->d_red_out);
     h->device_bytes = 0;
@@ -219,8 +218,7 @@ int lbm_set_geometry(LbmHandle* h, const int8_t* solid) {
         rc = rc ? rc : dev_alloc(h, &h->d_rr[1], rbytes * h->np, "rho_r B");
         rc = rc ? rc : dev_alloc(h, &h->d_rb[0], rbytes * h->np, "rho_b A");
         rc = rc ? rc : dev_alloc(h, &h->d_rb[1], rbytes * h->np, "rho_b B");
-        rc = rc ? rc : dev_alloc(h, &h->d_cg, rbytes * 3 * h->np, "colour gradient");
-        rc = rc ? rc : dev_alloc(h, &h->d_psi_dense, sizeof(float) * nc, "psi dense");
+        rc = rc ? rc : dev_alloc(h, &h->d_cs, rbytes * 9 * h->np, "recolouring amounts");
     }
     h->red_blocks = (int)std::min<int64_t>(4 * h->sm_count, (h->n_fluid + 255) / 256 + 1);
     rc = rc ? rc : dev_alloc(h, &h->d_red, sizeof(double) * 8 * h->red_blocks, "reduction partials");
@@ -378,8 +376,11 @@ int lbm_get_phase(LbmHandle* h, float* psi, float* rho_r, float* rho_b) {
     cudaSetDevice(h->device);
     int rc = LBM_OK;
     if (psi) {
-        rc = lbm_cuda_check(h, cudaMemcpyAsync(psi, h->d_psi_dense, sizeof(float) * h->ncell, cudaMemcpyDeviceToHost, h->stream), "copy psi");
-        if (!rc) rc = lbm_cuda_check(h, cudaStreamSynchronize(h->stream), "copy psi");
+        // fluid cells from the device; solid cells keep the input psi (the reference never updates them)
+        std::vector<float> fl(h->ncell);
+        rc = scatter_dense<float>(h, h->d_psi, 1, fl.data(), 0.0f);
+        if (!rc)
+            for (int64_t c = 0; c < h->ncell; ++c) psi[c] = h->solid[c] ? h->psi0[c] : fl[c];
     }
     if (!rc && rho_r) rc = scatter_dense<float>(h, h->d_rr[h->ccur], 1, rho_r, 0.0f);
     if (!rc && rho_b) rc = scatter_dense<float>(h, h->d_rb[h->ccur], 1, rho_b, 0.0f);

@@ -56,8 +56,7 @@ struct LbmHandle {
     void* d_psi = nullptr;                 // [np] psi at fluid nodes
     void* d_rr[2] = {nullptr, nullptr};    // rho_r, double-buffered [np]
     void* d_rb[2] = {nullptr, nullptr};    // rho_b
-    void* d_cg = nullptr;                  // colour gradient C [3][np]
-    float* d_psi_dense = nullptr;          // dense psi of every cell (solid cells keep input)
+    void* d_cs = nullptr;                  // recolouring amounts of the 9 pairs [9][np]
     int ccur = 0;
     // reductions
     double* d_red = nullptr;               // per-block partials

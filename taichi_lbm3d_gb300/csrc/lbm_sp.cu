@@ -19,6 +19,7 @@
 
 #include "lbm_common.cuh"
 #include "lbm_internal.h"
+#include "lbm_kernels.cuh"
 
 // Resident CTAs per SM requested for the unforced FP32/16-bit step kernel
 // (caps registers at 65536 / (256 * LBM_SP_MINBLOCKS)).
@@ -27,194 +28,7 @@
 #endif
 
 namespace {
-
-// Pull sources.  For node x and direction S the population comes from the
-// node at x - e_S (periodic wrap, SP:247-257), or -- when that cell is solid --
-// from the node's own LR[S] slot (halfway bounce-back, SP:265-268).  The cell is
-// looked up in the dense map through 9 row offsets (one per (y, z) pair); when
-// no lane of the warp sits on an x face the x neighbours are at +-1 from the
-// row offset, so each lookup is one load with an immediate offset.
-struct Rows {
-    int r[3][3];  // [source y: j-1, j, j+1 wrapped][source z], cell index of (i, y, z)
-};
-
-__device__ __forceinline__ Rows make_rows(int nx, int ny, int i, int j, int k, int ym, int yp, int zm, int zp) {
-    Rows R;
-    const int ys[3] = {ym, j, yp};
-    const int zs[3] = {zm, k, zp};
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-#pragma unroll
-        for (int b = 0; b < 3; ++b) R.r[a][b] = i + nx * (ys[a] + ny * zs[b]);
-    return R;
-}
-
-template <int STORE, bool XWRAP>
-struct Gather {
-    using Cd = Codec<STORE>;
-    using T = typename Cd::T;
-    using R = typename Cd::R;
-    template <int S>
-    static __device__ __forceinline__ void one(R* F, const T* __restrict__ fin, const T* __restrict__ own,
-                                               const int32_t* __restrict__ map, const Rows& rows, int i, int xm,
-                                               int xp) {
-        constexpr int ex = lbm_ex(S), ey = lbm_ey(S), ez = lbm_ez(S);
-        // source is x - e_S: row index 0 holds y-1 (used when ey = +1)
-        const int row = rows.r[1 - ey][1 - ez];
-        int src;
-        if constexpr (XWRAP) {
-            const int x = ex > 0 ? xm : (ex < 0 ? xp : i);
-            src = __ldg(map + (row - i + x));
-        } else {
-            src = __ldg(map + row - ex);
-        }
-        if (src >= 0) F[S] = Cd::template dec<S>(fin[lbm_eoff32(src) + 32 * S]);
-        else F[S] = Cd::template dec<S>(own[32 * lbm_lr(S)]);
-    }
-    static __device__ __forceinline__ void all(R* F, const T* __restrict__ fin, const T* __restrict__ own,
-                                               const int32_t* __restrict__ map, const Rows& rows, int i, int xm,
-                                               int xp) {
-        F[0] = Cd::template dec<0>(own[0]);
-#define LBM_G(S) one<S>(F, fin, own, map, rows, i, xm, xp);
-        LBM_G(1) LBM_G(2) LBM_G(3) LBM_G(4) LBM_G(5) LBM_G(6) LBM_G(7) LBM_G(8) LBM_G(9)
-        LBM_G(10) LBM_G(11) LBM_G(12) LBM_G(13) LBM_G(14) LBM_G(15) LBM_G(16) LBM_G(17) LBM_G(18)
-#undef LBM_G
-    }
-};
-
-// Gather F for node n; warps with no lane on an x face take the immediate-offset path.
-template <int STORE>
-__device__ __forceinline__ void gather_node(typename Codec<STORE>::R* F, const typename Codec<STORE>::T* __restrict__ fin,
-                                            const int32_t* __restrict__ map, int n, int nx, int ny, int nz, int i, int j,
-                                            int k) {
-    const int xm = i == 0 ? nx - 1 : i - 1, xp = i == nx - 1 ? 0 : i + 1;
-    const int ym = j == 0 ? ny - 1 : j - 1, yp = j == ny - 1 ? 0 : j + 1;
-    const int zm = k == 0 ? nz - 1 : k - 1, zp = k == nz - 1 ? 0 : k + 1;
-    const Rows rows = make_rows(nx, ny, i, j, k, ym, yp, zm, zp);
-    const typename Codec<STORE>::T* own = fin + lbm_eoff32(n);
-    const bool x_inside = i > 0 && i < nx - 1;
-    if (__all_sync(__activemask(), x_inside)) Gather<STORE, false>::all(F, fin, own, map, rows, i, xm, xp);
-    else Gather<STORE, true>::all(F, fin, own, map, rows, i, xm, xp);
-}
-
-#define LBM_ALL_DIRS(X) X(1) X(2) X(3) X(4) X(5) X(6) X(7) X(8) X(9) X(10) X(11) X(12) X(13) X(14) X(15) X(16) X(17) X(18)
-
-// v component sums: sum_s e_s[c] F[s] with zero terms dropped (SP:382-383).
-template <int C, typename R>
-__device__ __forceinline__ R vsum(const R* F) {
-    R a = (R)0;
-    bool first = true;
-#pragma unroll
-    for (int s = 1; s < 19; ++s) {
-        const int e = C == 0 ? lbm_ex(s) : (C == 1 ? lbm_ey(s) : lbm_ez(s));
-        if (e == 0) continue;
-        if (first) { a = e > 0 ? F[s] : -F[s]; first = false; }
-        else a = e > 0 ? a + F[s] : a - F[s];
-    }
-    return a;
-}
-
-// Class collision (SP:222-241): F, rho, v -> f (in place).
-template <typename R, bool FORCE>
-__device__ __forceinline__ void collide_sp(R* F, R r, R vx, R vy, R vz, const SpConsts<R>& C) {
-    R m[19];
-    mrt_moments<R>(F, m);
-    const R uu = lbm_usq(vx, vy, vz);
-    R meq[19];
-#pragma unroll
-    for (int s = 0; s < 19; ++s) meq[s] = (R)0;
-    meq[0] = r; meq[3] = vx; meq[5] = vy; meq[7] = vz; meq[1] = uu;
-    meq[9] = (((R)2 * vx) * vx - vy * vy) - vz * vz;
-    meq[11] = vy * vy - vz * vz;
-    meq[13] = vx * vy; meq[14] = vy * vz; meq[15] = vx * vz;
-#pragma unroll
-    for (int s = 0; s < 19; ++s) {
-        const int kd = lbm_skind(s);
-        if (kd == 0) continue;
-        const R S = kd == 1 ? C.sv : C.so;
-        m[s] = m[s] - S * (m[s] - meq[s]);
-    }
-    if constexpr (FORCE) {
-        const R fx = C.fext[0], fy = C.fext[1], fz = C.fext[2];
-        R G[19];
-#pragma unroll
-        for (int l = 0; l < 19; ++l) {
-            R a = ((R)lbm_ex(l) - vx) * fx;
-            a = a + ((R)lbm_ey(l) - vy) * fy;
-            a = a + ((R)lbm_ez(l) - vz) * fz;
-            R eu, ef;
-            switch (l) {
-#define LBM_EU(S) case S: eu = lbm_edot<S, R>(vx, vy, vz); ef = lbm_edot<S, R>(fx, fy, fz); break;
-                LBM_EU(0) LBM_EU(1) LBM_EU(2) LBM_EU(3) LBM_EU(4) LBM_EU(5) LBM_EU(6) LBM_EU(7) LBM_EU(8) LBM_EU(9)
-                LBM_EU(10) LBM_EU(11) LBM_EU(12) LBM_EU(13) LBM_EU(14) LBM_EU(15) LBM_EU(16) LBM_EU(17) LBM_EU(18)
-#undef LBM_EU
-            }
-            R g;
-            if (C.guo == 0) g = a / (R)3.0 + (eu * ef) / (R)9.0;   // class (SP:236)
-            else if (C.guo == 1) g = a + eu * ef;                  // scripts (TP:246)
-            else g = (R)3.0 * a + (R)9.0 * (eu * ef);              // standard Guo, c_s^2 = 1/3
-            G[l] = (R)lbm_w(l) * g;
-        }
-        R fg[19];
-        mrt_moments<R>(G, fg);
-#pragma unroll
-        for (int s = 0; s < 19; ++s) {
-            const int kd = lbm_skind(s);
-            const R S = kd == 0 ? (R)0 : (kd == 1 ? C.sv : C.so);
-            m[s] = m[s] + ((R)1 - (R)0.5 * S) * fg[s];
-        }
-    }
-    mrt_back<R>(m, F);
-}
-
-// Face boundary conditions for one node on >= 1 non-periodic face
-// (SP:272-370; script velocity form TP:502-506).  Faces in reference order;
-// a later face overwrites what an earlier one wrote (edges, corners).
-template <typename R>
-__device__ __forceinline__ void apply_faces(R* F, int i, int j, int k, int n, const SpConsts<R>& C,
-                                            const int32_t* __restrict__ map, const R* __restrict__ vprev) {
-#pragma unroll 1
-    for (int f = 0; f < 6; ++f) {
-        const int bc = C.bc[f];
-        if (bc == 0) continue;
-        const int hi = f & 1;
-        const int c = f < 2 ? i : (f < 4 ? j : k);
-        const int nmax = f < 2 ? C.nx : (f < 4 ? C.ny : C.nz);
-        if (c != (hi ? nmax - 1 : 0)) continue;
-        R fe[19];
-        if (bc == LBM_BC_PRESSURE) {
-            const int inw = hi ? nmax - 2 : 1;
-            const int qi = f < 2 ? inw : i, qj = (f >= 2 && f < 4) ? inw : j, qk = f >= 4 ? inw : k;
-            const bool in_solid = __ldg(map + qi + C.nx * (qj + C.ny * qk)) < 0;
-            R u0 = (R)0, u1 = (R)0, u2 = (R)0;
-            if (!in_solid) {
-                u0 = vprev[n];
-                u1 = vprev[C.np + n];
-                u2 = vprev[2 * C.np + n];
-            }
-            lbm_feq_all<R>(C.rho_bc[f], u0, u1, u2, fe);
-#pragma unroll
-            for (int s = 0; s < 19; ++s) F[s] = fe[s];
-        } else {
-            lbm_feq_all<R>((R)1.0, C.vel_bc[f][0], C.vel_bc[f][1], C.vel_bc[f][2], fe);
-            if (C.bc_form == 0) {
-#pragma unroll
-                for (int s = 0; s < 19; ++s) F[s] = fe[s];
-            } else {
-#pragma unroll
-                for (int s = 0; s < 19; ++s) F[s] = (fe[lbm_lr(s)] - F[lbm_lr(s)]) + fe[s];
-            }
-        }
-    }
-}
-
-template <typename R>
-__device__ __forceinline__ bool on_face(int i, int j, int k, const SpConsts<R>& C, bool pressure_only) {
-    const int code = pressure_only ? LBM_BC_PRESSURE : -1;
-    auto hit = [&](int f, bool at) { return at && C.bc[f] != 0 && (code < 0 || C.bc[f] == code); };
-    return hit(0, i == 0) || hit(1, i == C.nx - 1) || hit(2, j == 0) || hit(3, j == C.ny - 1) || hit(4, k == 0) ||
-           hit(5, k == C.nz - 1);
-}
+using namespace lbmk;
 
 template <int STORE, bool FORCE, bool MACROS>
 __global__ void __launch_bounds__(256, STORE == LBM_STORE_F64 ? 1 : (FORCE ? 4 : LBM_SP_MINBLOCKS)) sp_step_kernel(const __grid_constant__ SpConsts<typename Codec<STORE>::R> C,
