@@ -197,6 +197,37 @@ def cpu_baseline(solid, max_seconds=20.0):
             "sample": "%d steps of the full 256^3 workload (%.1f s)" % (n, t)}
 
 
+def convergence(storages=("f64", "f32", "f32dev", "f16", "bf16"), tol=1e-6, check_every=500, max_steps=200_000,
+                shape=SHAPE, visc="standard"):
+    """Config 2 run to steady state: |dk/k| <= tol over check_every steps.
+    Each storage variant reports steps, wall time and its permeability error
+    against the FP64 run of the same solver."""
+    from taichi_lbm3d_gb300 import LB3D_Solver_Single_Phase
+    solid = geometry() if shape == SHAPE else None
+    if solid is None:
+        from taichi_lbm3d_gb300.geometry import sphere_pack
+        solid = sphere_pack(shape, PACK["rmin"], PACK["rmax"], PACK["porosity"], PACK["seed"])
+    out = {}
+    for sto in storages:
+        lb = LB3D_Solver_Single_Phase(*shape, storage=sto, viscosity_convention=visc, guo_convention="standard")
+        lb.solid.from_numpy(solid)
+        lb.set_viscosity(NIU)
+        lb.set_bc_rho_x0(RHO_IN)
+        lb.set_bc_rho_x1(RHO_OUT)
+        lb.init_simulation()
+        t0 = time.perf_counter()
+        r = lb.run_to_convergence(tol=tol, check_every=check_every, max_steps=max_steps)
+        secs = time.perf_counter() - t0
+        r.update(seconds=secs, mlups=lb.n_fluid * r["steps"] / secs / 1e6)
+        lb.close()
+        out[sto] = r
+    if "f64" in out:
+        k64 = out["f64"]["k"]
+        for sto, r in out.items():
+            r["k_rel_err_vs_f64"] = abs(r["k"] - k64) / abs(k64)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -205,7 +236,14 @@ def main():
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--convergence", action="store_true",
+                    help="run the 256^3 pack to steady state in FP64/FP32/FP16/BF16 and print k errors")
     a = ap.parse_args()
+    if a.convergence:
+        res = convergence()
+        print(json.dumps({"convergence": res, "config": workload_config(), "tol": 1e-6, "check_every": 500,
+                          "viscosity_convention": "standard (tau = 3 niu + 1/2)"}))
+        return 0
     warmup = max(3, a.warmup)
 
     rank = int(os.environ.get("RANK", "0"))

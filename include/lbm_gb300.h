@@ -46,12 +46,17 @@ enum {
  * Face order everywhere: x-left, x-right, y-left, y-right, z-left, z-right. */
 enum { LBM_BC_PERIODIC = 0, LBM_BC_PRESSURE = 1, LBM_BC_VELOCITY = 2 };
 
-/* Population storage of the fused kernels. */
+/* Population storage of the fused kernels.  F32 and F64 compute on f itself,
+ * as the reference does (F32 reproduces its FP32 rounding bit for bit).  The
+ * *_DEV modes compute in FP32 on f - w and rho - 1 (deviation form); F16_DEV and
+ * BF16_DEV store each node's populations relative to its own density,
+ * g = f - w*rho_node, with rho_node - 1 kept per node in FP32. */
 enum {
-    LBM_STORE_F32 = 0,       /* plain FP32 populations */
-    LBM_STORE_F16_DEV = 1,   /* FP16 of (f_s - w_s)*2^12, collide in FP32 */
-    LBM_STORE_BF16_DEV = 2,  /* BF16 of (f_s - w_s), collide in FP32 */
-    LBM_STORE_F64 = 3        /* FP64 populations and arithmetic (accuracy reference) */
+    LBM_STORE_F32 = 0,       /* FP32 f, reference arithmetic */
+    LBM_STORE_F16_DEV = 1,   /* FP16 of g * 2^16, deviation-form FP32 collide */
+    LBM_STORE_BF16_DEV = 2,  /* BF16 of g, deviation-form FP32 collide */
+    LBM_STORE_F64 = 3,       /* FP64 f and arithmetic (accuracy reference) */
+    LBM_STORE_F32_DEV = 4    /* FP32 of f - w, deviation-form FP32 collide */
 };
 
 /* Solver parameters: the attributes the reference's class sets before
@@ -146,6 +151,15 @@ int lbm_get_max_v(LbmHandle* h, float* out);
 int lbm_reductions(LbmHandle* h, LbmStats* out);
 
 int lbm_get_info(LbmHandle* h, LbmInfo* out);
+
+/* Permeability driver (no counterpart in the reference, whose examples loop on
+ * step() and print get_max_v): run until the FP64 Darcy velocity along `axis`
+ * (sum of v over fluid nodes / all cells, proportional to the permeability)
+ * changes by at most tol (relative) between checks `check_every` steps apart,
+ * or until max_steps.  Outputs the last Darcy velocity, the steps taken and
+ * whether the criterion was met.  Returns LBM_EDIVERGED on NaN/Inf. */
+int lbm_run_to_convergence(LbmHandle* h, double tol, int32_t check_every, int64_t max_steps, int32_t axis,
+                           double* darcy_v, int64_t* steps, int32_t* converged);
 
 /* Compacted fluid index: cell id of each fluid node, in node order (n_fluid). */
 int lbm_get_fluid_index(LbmHandle* h, int32_t* cell_of_node);

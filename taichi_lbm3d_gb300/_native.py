@@ -12,7 +12,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "liblbm_gb300.so")
 
 LBM_OK, LBM_EINVAL, LBM_ENODEV, LBM_ENOMEM, LBM_ECUDA, LBM_ESTATE, LBM_EDIVERGED = 0, -1, -2, -3, -4, -5, -6
-STORE = {"f32": 0, "f16": 1, "bf16": 2, "f64": 3}
+STORE = {"f32": 0, "f16": 1, "bf16": 2, "f64": 3, "f32dev": 4}
 STORE_NAME = {v: k for k, v in STORE.items()}
 
 
@@ -74,6 +74,9 @@ SIGNATURES = {
     "lbm_get_max_v": [_P, ctypes.POINTER(ctypes.c_float)],
     "lbm_reductions": [_P, ctypes.POINTER(LbmStats)],
     "lbm_get_info": [_P, ctypes.POINTER(LbmInfo)],
+    "lbm_run_to_convergence": [_P, ctypes.c_double, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32,
+                               ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64),
+                               ctypes.POINTER(ctypes.c_int32)],
     "lbm_get_fluid_index": [_P, _P],
     "lbm_get_neighbors": [_P, _P],
     "lbm_get_populations": [_P, _P],
@@ -206,6 +209,13 @@ class Lattice:
         st = LbmStats()
         self._c(load().lbm_reductions(self.h, ctypes.byref(st)))
         return st
+
+    def run_to_convergence(self, tol=1e-6, check_every=500, max_steps=1_000_000, axis=0):
+        """Step until the FP64 Darcy velocity changes by <= tol between checks."""
+        dv, st, cv = ctypes.c_double(), ctypes.c_int64(), ctypes.c_int32()
+        self._c(load().lbm_run_to_convergence(self.h, float(tol), int(check_every), int(max_steps), int(axis),
+                                              ctypes.byref(dv), ctypes.byref(st), ctypes.byref(cv)))
+        return dv.value, st.value, bool(cv.value)
 
     def info(self):
         inf = LbmInfo()

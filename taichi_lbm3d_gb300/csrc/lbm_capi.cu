@@ -50,6 +50,8 @@ void free_lattice(LbmHandle* h) {
     dev_free(h->d_vprev);
     dev_free(h->d_rho);
     dev_free(h->d_v);
+    dev_free(h->d_rref[0]);
+    dev_free(h->d_rref[1]);
     dev_free(h->d_psi);
     dev_free(h->d_rr[0]);
     dev_free(h->d_rr[1]);
@@ -67,6 +69,7 @@ size_t store_elem(int storage) {
     case LBM_STORE_F16_DEV: return 2;
     case LBM_STORE_BF16_DEV: return 2;
     case LBM_STORE_F64: return 8;
+    case LBM_STORE_F32_DEV: return 4;
     }
     return 0;
 }
@@ -212,6 +215,10 @@ int lbm_set_geometry(LbmHandle* h, const int8_t* solid) {
     rc = rc ? rc : dev_alloc(h, &h->d_vprev, rbytes * 3 * h->np, "vprev");
     rc = rc ? rc : dev_alloc(h, &h->d_rho, rbytes * h->np, "rho");
     rc = rc ? rc : dev_alloc(h, &h->d_v, rbytes * 3 * h->np, "v");
+    if (h->p.storage == LBM_STORE_F16_DEV || h->p.storage == LBM_STORE_BF16_DEV) {
+        rc = rc ? rc : dev_alloc(h, &h->d_rref[0], sizeof(float) * h->np, "node density A");
+        rc = rc ? rc : dev_alloc(h, &h->d_rref[1], sizeof(float) * h->np, "node density B");
+    }
     if (!rc && h->p.two_phase) {
         rc = rc ? rc : dev_alloc(h, &h->d_psi, rbytes * h->np, "psi");
         rc = rc ? rc : dev_alloc(h, &h->d_rr[0], rbytes * h->np, "rho_r A");
@@ -411,6 +418,43 @@ int lbm_get_max_v(LbmHandle* h, float* out) {
     return red_launch(h, &st, out);
 }
 
+int lbm_run_to_convergence(LbmHandle* h, double tol, int32_t check_every, int64_t max_steps, int32_t axis,
+                           double* darcy_v, int64_t* steps, int32_t* converged) {
+    if (!h || !darcy_v || !steps || !converged) return lbm_set_err(h, LBM_EINVAL, "lbm_run_to_convergence: NULL argument");
+    if (check_every < 1 || max_steps < 1 || axis < 0 || axis > 2 || !(tol >= 0))
+        return lbm_set_err(h, LBM_EINVAL, "lbm_run_to_convergence: bad tol / check_every / max_steps / axis");
+    if (!h->initialized) return lbm_set_err(h, LBM_ESTATE, "lbm_run_to_convergence: call lbm_init first");
+    cudaSetDevice(h->device);
+    double prev = 0.0, vm = 0.0;
+    bool have_prev = false;
+    int64_t done = 0;
+    *converged = 0;
+    while (done < max_steps) {
+        const int32_t n = (int32_t)std::min<int64_t>(check_every, max_steps - done);
+        int rc = lbm_step_async(h, n);
+        if (rc) return rc;
+        done += n;
+        LbmStats st;
+        rc = red_launch(h, &st, nullptr);
+        if (rc) return rc;
+        if (st.n_nonfinite) {
+            *darcy_v = NAN;
+            *steps = done;
+            return lbm_set_err(h, LBM_EDIVERGED, "lbm_run_to_convergence: non-finite rho or v");
+        }
+        vm = st.mom[axis] / (double)h->ncell;
+        if (have_prev && std::fabs(vm - prev) <= tol * std::fabs(vm)) {
+            *converged = 1;
+            break;
+        }
+        prev = vm;
+        have_prev = true;
+    }
+    *darcy_v = vm;
+    *steps = done;
+    return LBM_OK;
+}
+
 int lbm_get_info(LbmHandle* h, LbmInfo* out) {
     if (!h || !out) return lbm_set_err(h, LBM_EINVAL, "lbm_get_info: NULL argument");
     out->n_cells = h->ncell;
@@ -463,6 +507,12 @@ int lbm_get_populations(LbmHandle* h, double* f) {
     std::vector<unsigned char> tmp(h->elem * 19 * h->np);
     int rc = lbm_cuda_check(h, cudaMemcpy(tmp.data(), h->d_f[h->cur], tmp.size(), cudaMemcpyDeviceToHost), "copy f");
     if (rc) return rc;
+    std::vector<float> rr;
+    if (h->d_rref[h->cur]) {
+        rr.resize(h->np);
+        rc = lbm_cuda_check(h, cudaMemcpy(rr.data(), h->d_rref[h->cur], sizeof(float) * h->np, cudaMemcpyDeviceToHost), "copy rho'");
+        if (rc) return rc;
+    }
     for (int s = 0; s < 19; ++s)
         for (int32_t n = 0; n < h->n_fluid; ++n) {
             const int64_t idx = lbm_pidx(n, s);
@@ -470,8 +520,13 @@ int lbm_get_populations(LbmHandle* h, double* f) {
             switch (h->p.storage) {
             case LBM_STORE_F32: val = ((const float*)tmp.data())[idx]; break;
             case LBM_STORE_F64: val = ((const double*)tmp.data())[idx]; break;
-            case LBM_STORE_F16_DEV: val = lbm_w(s) + (double)__half2float(((const __half*)tmp.data())[idx]) / 4096.0; break;
-            case LBM_STORE_BF16_DEV: val = lbm_w(s) + (double)__bfloat162float(((const __nv_bfloat16*)tmp.data())[idx]); break;
+            case LBM_STORE_F32_DEV: val = lbm_w(s) + (double)((const float*)tmp.data())[idx]; break;
+            case LBM_STORE_F16_DEV:
+                val = lbm_w(s) * (1.0 + rr[n]) + (double)__half2float(((const __half*)tmp.data())[idx]) / 65536.0;
+                break;
+            case LBM_STORE_BF16_DEV:
+                val = lbm_w(s) * (1.0 + rr[n]) + (double)__bfloat162float(((const __nv_bfloat16*)tmp.data())[idx]);
+                break;
             }
             f[(int64_t)s * h->n_fluid + n] = val;
         }
@@ -482,18 +537,28 @@ int lbm_set_populations(LbmHandle* h, const double* f) {
     if (!h || !f) return lbm_set_err(h, LBM_EINVAL, "lbm_set_populations: NULL argument");
     if (!h->initialized || h->p.two_phase) return lbm_set_err(h, LBM_ESTATE, "lbm_set_populations: needs an initialised single-phase handle");
     std::vector<unsigned char> tmp(h->elem * 19 * h->np, 0);
+    std::vector<float> rr(h->np, 0.0f);
+    for (int32_t n = 0; n < h->n_fluid; ++n) {   // node density for the RHOREF encodings
+        double r = 0;
+        for (int s = 0; s < 19; ++s) r += f[(int64_t)s * h->n_fluid + n];
+        rr[n] = (float)(r - 1.0);
+    }
     for (int s = 0; s < 19; ++s)
         for (int32_t n = 0; n < h->n_fluid; ++n) {
             const int64_t idx = lbm_pidx(n, s);
             const double val = f[(int64_t)s * h->n_fluid + n];
+            const double g = val - lbm_w(s) * (1.0 + (double)rr[n]);
             switch (h->p.storage) {
             case LBM_STORE_F32: ((float*)tmp.data())[idx] = (float)val; break;
             case LBM_STORE_F64: ((double*)tmp.data())[idx] = val; break;
-            case LBM_STORE_F16_DEV: ((__half*)tmp.data())[idx] = __float2half_rn((float)((val - lbm_w(s)) * 4096.0)); break;
-            case LBM_STORE_BF16_DEV: ((__nv_bfloat16*)tmp.data())[idx] = __float2bfloat16_rn((float)(val - lbm_w(s))); break;
+            case LBM_STORE_F32_DEV: ((float*)tmp.data())[idx] = (float)(val - lbm_w(s)); break;
+            case LBM_STORE_F16_DEV: ((__half*)tmp.data())[idx] = __float2half_rn((float)(g * 65536.0)); break;
+            case LBM_STORE_BF16_DEV: ((__nv_bfloat16*)tmp.data())[idx] = __float2bfloat16_rn((float)g); break;
             }
         }
     int rc = lbm_cuda_check(h, cudaMemcpy(h->d_f[h->cur], tmp.data(), tmp.size(), cudaMemcpyHostToDevice), "copy f");
+    if (!rc && h->d_rref[h->cur])
+        rc = lbm_cuda_check(h, cudaMemcpy(h->d_rref[h->cur], rr.data(), sizeof(float) * h->np, cudaMemcpyHostToDevice), "copy rho'");
     h->macros_valid = false;
     return rc;
 }

@@ -106,34 +106,65 @@ __device__ __forceinline__ void lbm_feq_all(R rho, R u0, R u1, R u2, R* out) {
 }
 
 // ---------------------------------------------------------------- storage
-// Population codecs: Codec<STORE>::T is the stored element type; R the compute
-// type.  Deviation storage keeps f_s - w_s (rho0 = 1), scaled by 2^12 in FP16
-// so that deviations down to ~1e-8 stay in FP16's normal range.
+// Population codecs: Codec<STORE>::T is the stored element type, R the compute
+// type.  DEV codecs compute in deviation form: the kernel works on
+// f' = f - w and rho' = rho - 1 (the transforms are linear and M w is the unit
+// vector of moment 0, so only moment 0 and the macroscopic density change),
+// which keeps the small flow signal out of the rounding of f ~ w.  RHOREF
+// codecs store each node's post-collision populations relative to its own
+// density, g = f' - w rho'_node, with rho'_node kept per node in FP32; the
+// reader adds w rho'_source back.  What is left in g is the velocity and
+// non-equilibrium part, which 16-bit storage can resolve (FP16 scaled by 2^16:
+// |g| from ~1e-9 to 1 keeps 11 significant bits).
 template <int STORE> struct Codec;
 template <> struct Codec<LBM_STORE_F32> {
     using T = float; using R = float;
+    static constexpr bool DEV = false, RHOREF = false;
     template <int S> static __device__ __forceinline__ R dec(T x) { return x; }
     template <int S> static __device__ __forceinline__ T enc(R f) { return f; }
 };
 template <> struct Codec<LBM_STORE_F64> {
     using T = double; using R = double;
+    static constexpr bool DEV = false, RHOREF = false;
+    template <int S> static __device__ __forceinline__ R dec(T x) { return x; }
+    template <int S> static __device__ __forceinline__ T enc(R f) { return f; }
+};
+template <> struct Codec<LBM_STORE_F32_DEV> {
+    using T = float; using R = float;
+    static constexpr bool DEV = true, RHOREF = false;
     template <int S> static __device__ __forceinline__ R dec(T x) { return x; }
     template <int S> static __device__ __forceinline__ T enc(R f) { return f; }
 };
 template <> struct Codec<LBM_STORE_F16_DEV> {
     using T = __half; using R = float;
-    template <int S> static __device__ __forceinline__ R dec(T x) {
-        return __fmaf_rn(__half2float(x), 1.0f / 4096.0f, (float)lbm_w(S));
-    }
-    template <int S> static __device__ __forceinline__ T enc(R f) {
-        return __float2half_rn((f - (float)lbm_w(S)) * 4096.0f);
-    }
+    static constexpr bool DEV = true, RHOREF = true;
+    template <int S> static __device__ __forceinline__ R dec(T x) { return __half2float(x) * (1.0f / 65536.0f); }
+    template <int S> static __device__ __forceinline__ T enc(R g) { return __float2half_rn(g * 65536.0f); }
 };
 template <> struct Codec<LBM_STORE_BF16_DEV> {
     using T = __nv_bfloat16; using R = float;
-    template <int S> static __device__ __forceinline__ R dec(T x) { return __bfloat162float(x) + (float)lbm_w(S); }
-    template <int S> static __device__ __forceinline__ T enc(R f) { return __float2bfloat16_rn(f - (float)lbm_w(S)); }
+    static constexpr bool DEV = true, RHOREF = true;
+    template <int S> static __device__ __forceinline__ R dec(T x) { return __bfloat162float(x); }
+    template <int S> static __device__ __forceinline__ T enc(R g) { return __float2bfloat16_rn(g); }
 };
+
+// feq_S(rho, u) - w_S with rho = 1 + rho' (deviation form of lbm_feq).
+template <int S, typename R>
+LBM_HD R lbm_feq_dev(R rho_dev, R u0, R u1, R u2, R uv) {
+    R eu = lbm_edot<S, R>(u0, u1, u2);
+    R t = (R)3.0 * eu + ((R)4.5 * eu) * eu;
+    t = t - (R)1.5 * uv;
+    return (R)lbm_w(S) * (rho_dev + ((R)1 + rho_dev) * t);
+}
+
+template <typename R>
+__device__ __forceinline__ void lbm_feq_dev_all(R rho_dev, R u0, R u1, R u2, R* out) {
+    const R uv = lbm_usq(u0, u1, u2);
+#define LBM_FQ(S) out[S] = lbm_feq_dev<S, R>(rho_dev, u0, u1, u2, uv);
+    LBM_FQ(0) LBM_FQ(1) LBM_FQ(2) LBM_FQ(3) LBM_FQ(4) LBM_FQ(5) LBM_FQ(6) LBM_FQ(7) LBM_FQ(8) LBM_FQ(9)
+    LBM_FQ(10) LBM_FQ(11) LBM_FQ(12) LBM_FQ(13) LBM_FQ(14) LBM_FQ(15) LBM_FQ(16) LBM_FQ(17) LBM_FQ(18)
+#undef LBM_FQ
+}
 
 // Population layout "AoSoA-32": nodes in chunks of 32; within a chunk the 19
 // directions follow one another, 32 consecutive nodes each.  Element (n, s) is

@@ -20,6 +20,7 @@ struct SpConsts {
     int32_t any_pressure;
     int32_t guo;
     R rho_bc[6];
+    R rho_bc_dev[6];   // rho_bc - 1, rounded once from FP64
     R vel_bc[6][3];
     R sv, so;          // S_dig values s_v, s_other (SP:128-131)
     R fext[3];
@@ -52,6 +53,7 @@ struct LbmHandle {
     void* d_vprev = nullptr;               // [3][np] previous-step v (pressure faces)
     void* d_rho = nullptr;                 // [np]
     void* d_v = nullptr;                   // [3][np]
+    float* d_rref[2] = {nullptr, nullptr}; // RHOREF storage: rho - 1 per node, ping-pong with f
     // two phase
     void* d_psi = nullptr;                 // [np] psi at fluid nodes
     void* d_rr[2] = {nullptr, nullptr};    // rho_r, double-buffered [np]

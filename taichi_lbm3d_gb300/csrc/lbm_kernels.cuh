@@ -37,7 +37,7 @@ struct Gather {
     template <int S>
     static __device__ __forceinline__ void one(R* F, const T* __restrict__ fin, const T* __restrict__ own,
                                                const int32_t* __restrict__ map, const Rows& rows, int i, int xm,
-                                               int xp) {
+                                               int xp, const float* __restrict__ rref, int n) {
         constexpr int ex = lbm_ex(S), ey = lbm_ey(S), ez = lbm_ez(S);
         // source is x - e_S: row index 0 holds y-1 (used when ey = +1)
         const int row = rows.r[1 - ey][1 - ez];
@@ -50,12 +50,14 @@ struct Gather {
         }
         if (src >= 0) F[S] = Cd::template dec<S>(fin[lbm_eoff32(src) + 32 * S]);
         else F[S] = Cd::template dec<S>(own[32 * lbm_lr(S)]);
+        if constexpr (Cd::RHOREF) F[S] = lbm_fma<R>((R)lbm_w(S), (R)rref[src >= 0 ? src : n], F[S]);
     }
     static __device__ __forceinline__ void all(R* F, const T* __restrict__ fin, const T* __restrict__ own,
                                                const int32_t* __restrict__ map, const Rows& rows, int i, int xm,
-                                               int xp) {
+                                               int xp, const float* __restrict__ rref, int n) {
         F[0] = Cd::template dec<0>(own[0]);
-#define LBM_G(S) one<S>(F, fin, own, map, rows, i, xm, xp);
+        if constexpr (Cd::RHOREF) F[0] = lbm_fma<R>((R)lbm_w(0), (R)rref[n], F[0]);
+#define LBM_G(S) one<S>(F, fin, own, map, rows, i, xm, xp, rref, n);
         LBM_G(1) LBM_G(2) LBM_G(3) LBM_G(4) LBM_G(5) LBM_G(6) LBM_G(7) LBM_G(8) LBM_G(9)
         LBM_G(10) LBM_G(11) LBM_G(12) LBM_G(13) LBM_G(14) LBM_G(15) LBM_G(16) LBM_G(17) LBM_G(18)
 #undef LBM_G
@@ -66,18 +68,38 @@ struct Gather {
 template <int STORE>
 __device__ __forceinline__ void gather_node(typename Codec<STORE>::R* F, const typename Codec<STORE>::T* __restrict__ fin,
                                             const int32_t* __restrict__ map, int n, int nx, int ny, int nz, int i, int j,
-                                            int k) {
+                                            int k, const float* __restrict__ rref = nullptr) {
     const int xm = i == 0 ? nx - 1 : i - 1, xp = i == nx - 1 ? 0 : i + 1;
     const int ym = j == 0 ? ny - 1 : j - 1, yp = j == ny - 1 ? 0 : j + 1;
     const int zm = k == 0 ? nz - 1 : k - 1, zp = k == nz - 1 ? 0 : k + 1;
     const Rows rows = make_rows(nx, ny, i, j, k, ym, yp, zm, zp);
     const typename Codec<STORE>::T* own = fin + lbm_eoff32(n);
     const bool x_inside = i > 0 && i < nx - 1;
-    if (__all_sync(__activemask(), x_inside)) Gather<STORE, false>::all(F, fin, own, map, rows, i, xm, xp);
-    else Gather<STORE, true>::all(F, fin, own, map, rows, i, xm, xp);
+    if (__all_sync(__activemask(), x_inside)) Gather<STORE, false>::all(F, fin, own, map, rows, i, xm, xp, rref, n);
+    else Gather<STORE, true>::all(F, fin, own, map, rows, i, xm, xp, rref, n);
 }
 
 #define LBM_ALL_DIRS(X) X(1) X(2) X(3) X(4) X(5) X(6) X(7) X(8) X(9) X(10) X(11) X(12) X(13) X(14) X(15) X(16) X(17) X(18)
+
+// Store node n's post-collision populations; RHOREF codecs store them relative
+// to the node's density (g = f' - w r, r = rho - 1) and keep r.
+template <int STORE>
+__device__ __forceinline__ void store_node(const typename Codec<STORE>::R* F, typename Codec<STORE>::T* __restrict__ fout,
+                                           int n, typename Codec<STORE>::R r, float* __restrict__ rref_out) {
+    using Cd = Codec<STORE>;
+    using R = typename Cd::R;
+    typename Cd::T* out = fout + lbm_eoff32(n);
+    if constexpr (Cd::RHOREF) {
+#define LBM_S(S) out[32 * S] = Cd::template enc<S>(lbm_fma<R>(-(R)lbm_w(S), r, F[S]));
+        LBM_S(0) LBM_ALL_DIRS(LBM_S)
+#undef LBM_S
+        rref_out[n] = (float)r;
+    } else {
+#define LBM_S(S) out[32 * S] = Cd::template enc<S>(F[S]);
+        LBM_S(0) LBM_ALL_DIRS(LBM_S)
+#undef LBM_S
+    }
+}
 
 // v component sums: sum_s e_s[c] F[s] with zero terms dropped (SP:382-383).
 template <int C, typename R>
@@ -94,7 +116,8 @@ __device__ __forceinline__ R vsum(const R* F) {
     return a;
 }
 
-// Class collision (SP:222-241): F, rho, v -> f (in place).
+// Class collision (SP:222-241): F, rho, v -> f (in place).  In deviation form
+// F holds f - w and r is rho - 1 (moment 0 of M (f - w)).
 template <typename R, bool FORCE>
 __device__ __forceinline__ void collide_sp(R* F, R r, R vx, R vy, R vz, const SpConsts<R>& C) {
     R m[19];
@@ -150,7 +173,7 @@ __device__ __forceinline__ void collide_sp(R* F, R r, R vx, R vy, R vz, const Sp
 // Face boundary conditions for one node on >= 1 non-periodic face
 // (SP:272-370; script velocity form TP:502-506).  Faces in reference order;
 // a later face overwrites what an earlier one wrote (edges, corners).
-template <typename R>
+template <typename R, bool DEV = false>
 __device__ __forceinline__ void apply_faces(R* F, int i, int j, int k, int n, const SpConsts<R>& C,
                                             const int32_t* __restrict__ map, const R* __restrict__ vprev) {
 #pragma unroll 1
@@ -172,11 +195,14 @@ __device__ __forceinline__ void apply_faces(R* F, int i, int j, int k, int n, co
                 u1 = vprev[C.np + n];
                 u2 = vprev[2 * C.np + n];
             }
-            lbm_feq_all<R>(C.rho_bc[f], u0, u1, u2, fe);
+            if constexpr (DEV) lbm_feq_dev_all<R>(C.rho_bc_dev[f], u0, u1, u2, fe);
+            else lbm_feq_all<R>(C.rho_bc[f], u0, u1, u2, fe);
 #pragma unroll
             for (int s = 0; s < 19; ++s) F[s] = fe[s];
         } else {
-            lbm_feq_all<R>((R)1.0, C.vel_bc[f][0], C.vel_bc[f][1], C.vel_bc[f][2], fe);
+            // in deviation form the in-place form keeps its shape: the w terms cancel
+            if constexpr (DEV) lbm_feq_dev_all<R>((R)0, C.vel_bc[f][0], C.vel_bc[f][1], C.vel_bc[f][2], fe);
+            else lbm_feq_all<R>((R)1.0, C.vel_bc[f][0], C.vel_bc[f][1], C.vel_bc[f][2], fe);
             if (C.bc_form == 0) {
 #pragma unroll
                 for (int s = 0; s < 19; ++s) F[s] = fe[s];

@@ -38,7 +38,9 @@ __global__ void __launch_bounds__(256, STORE == LBM_STORE_F64 ? 1 : (FORCE ? 4 :
                                                       const uint32_t* __restrict__ coord,
                                                       typename Codec<STORE>::R* __restrict__ vprev,
                                                       typename Codec<STORE>::R* __restrict__ rho_out,
-                                                      typename Codec<STORE>::R* __restrict__ v_out) {
+                                                      typename Codec<STORE>::R* __restrict__ v_out,
+                                                      const float* __restrict__ rref_in,
+                                                      float* __restrict__ rref_out) {
     using Cd = Codec<STORE>;
     using R = typename Cd::R;
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
@@ -48,27 +50,28 @@ __global__ void __launch_bounds__(256, STORE == LBM_STORE_F64 ? 1 : (FORCE ? 4 :
     const int64_t np = C.np;
 
     R F[19];
-    gather_node<STORE>(F, fin, map, n, C.nx, C.ny, C.nz, i, j, k);
+    gather_node<STORE>(F, fin, map, n, C.nx, C.ny, C.nz, i, j, k, rref_in);
 
     // Face nodes are rare; warps without one skip the branch uniformly.
     bool face = false;
     if (C.any_bc) {
         face = on_face(i, j, k, C, false);
-        if (face) apply_faces<R>(F, i, j, k, n, C, map, vprev);
+        if (face) apply_faces<R, Cd::DEV>(F, i, j, k, n, C, map, vprev);
     }
 
-    // macros (SP:376-388)
+    // macros (SP:376-388); in deviation form r = rho - 1 and rho = 1 + r
     R r = F[0];
 #pragma unroll
     for (int s = 1; s < 19; ++s) r = r + F[s];
+    const R rho = Cd::DEV ? (R)1 + r : r;
     R vx = vsum<0>(F), vy = vsum<1>(F), vz = vsum<2>(F);
-    vx = vx / r;
-    vy = vy / r;
-    vz = vz / r;
+    vx = vx / rho;
+    vy = vy / rho;
+    vz = vz / rho;
     if constexpr (FORCE) {
-        vx = vx + C.fhalf[0] / r;
-        vy = vy + C.fhalf[1] / r;
-        vz = vz + C.fhalf[2] / r;
+        vx = vx + C.fhalf[0] / rho;
+        vy = vy + C.fhalf[1] / rho;
+        vz = vz + C.fhalf[2] / rho;
     }
     if (face && C.any_pressure && on_face(i, j, k, C, true)) {
         vprev[n] = vx;
@@ -76,17 +79,14 @@ __global__ void __launch_bounds__(256, STORE == LBM_STORE_F64 ? 1 : (FORCE ? 4 :
         vprev[2 * np + n] = vz;
     }
     if constexpr (MACROS) {
-        rho_out[n] = r;
+        rho_out[n] = rho;
         v_out[n] = vx;
         v_out[np + n] = vy;
         v_out[2 * np + n] = vz;
     }
 
     collide_sp<R, FORCE>(F, r, vx, vy, vz, C);
-    typename Cd::T* out = fout + lbm_eoff32(n);
-#define LBM_S(S) out[32 * S] = Cd::template enc<S>(F[S]);
-    LBM_S(0) LBM_ALL_DIRS(LBM_S)
-#undef LBM_S
+    store_node<STORE>(F, fout, n, r, rref_out);
 }
 
 // Initial populations: F = feq(rho, v), then one collision with (rho, v)
@@ -94,29 +94,29 @@ __global__ void __launch_bounds__(256, STORE == LBM_STORE_F64 ? 1 : (FORCE ? 4 :
 template <int STORE, bool FORCE>
 __global__ void sp_init_kernel(const __grid_constant__ SpConsts<typename Codec<STORE>::R> C,
                                typename Codec<STORE>::T* __restrict__ fout, const float* __restrict__ rho_in,
-                               const float* __restrict__ v_in, typename Codec<STORE>::R* __restrict__ vprev) {
+                               const float* __restrict__ v_in, typename Codec<STORE>::R* __restrict__ vprev,
+                               float* __restrict__ rref_out) {
     using Cd = Codec<STORE>;
     using R = typename Cd::R;
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= C.n_fluid) return;
     const int64_t np = C.np;
-    R r = (R)1.0, vx = (R)0, vy = (R)0, vz = (R)0;
+    R rd = (R)0, vx = (R)0, vy = (R)0, vz = (R)0;   // rho - 1 and v
     if (rho_in) {
-        r = (R)rho_in[n];
+        rd = (R)rho_in[n] - (R)1;
         vx = (R)v_in[n];
         vy = (R)v_in[np + n];
         vz = (R)v_in[2 * np + n];
     }
     R F[19];
-    lbm_feq_all<R>(r, vx, vy, vz, F);
+    if constexpr (Cd::DEV) lbm_feq_dev_all<R>(rd, vx, vy, vz, F);
+    else lbm_feq_all<R>((R)1 + rd, vx, vy, vz, F);
     vprev[n] = vx;
     vprev[np + n] = vy;
     vprev[2 * np + n] = vz;
+    const R r = Cd::DEV ? rd : (R)1 + rd;
     collide_sp<R, FORCE>(F, r, vx, vy, vz, C);
-    typename Cd::T* out = fout + lbm_eoff32(n);
-#define LBM_S(S) out[32 * S] = Cd::template enc<S>(F[S]);
-    LBM_S(0) LBM_ALL_DIRS(LBM_S)
-#undef LBM_S
+    store_node<STORE>(F, fout, n, r, rref_out);
 }
 
 // Pure pull-stream (identity collision, no faces): the permutation check.
@@ -140,7 +140,8 @@ int launch_step(LbmHandle* h, const SpConsts<typename Codec<STORE>::R>& C, int g
     const T* fin = (const T*)h->d_f[h->cur];
     T* fout = (T*)h->d_f[h->cur ^ 1];
     sp_step_kernel<STORE, FORCE, MACROS><<<grid, h->block, 0, h->stream>>>(
-        C, fin, fout, h->d_map, h->d_coord, (R*)h->d_vprev, (R*)h->d_rho, (R*)h->d_v);
+        C, fin, fout, h->d_map, h->d_coord, (R*)h->d_vprev, (R*)h->d_rho, (R*)h->d_v, h->d_rref[h->cur],
+        h->d_rref[h->cur ^ 1]);
     h->cur ^= 1;
     return lbm_cuda_check(h, cudaGetLastError(), "sp_step_kernel launch");
 }
@@ -167,8 +168,9 @@ int run_init(LbmHandle* h, const float* rho, const float* v) {
     const SpConsts<R> C = sp_make_consts<R>(h);
     const int grid = (int)((h->n_fluid + h->block - 1) / h->block);
     T* fout = (T*)h->d_f[h->cur];
-    if (h->force) sp_init_kernel<STORE, true><<<grid, h->block, 0, h->stream>>>(C, fout, rho, v, (R*)h->d_vprev);
-    else sp_init_kernel<STORE, false><<<grid, h->block, 0, h->stream>>>(C, fout, rho, v, (R*)h->d_vprev);
+    float* rref = h->d_rref[h->cur];
+    if (h->force) sp_init_kernel<STORE, true><<<grid, h->block, 0, h->stream>>>(C, fout, rho, v, (R*)h->d_vprev, rref);
+    else sp_init_kernel<STORE, false><<<grid, h->block, 0, h->stream>>>(C, fout, rho, v, (R*)h->d_vprev, rref);
     return lbm_cuda_check(h, cudaGetLastError(), "sp_init_kernel launch");
 }
 
@@ -187,6 +189,7 @@ SpConsts<R> sp_make_consts(const LbmHandle* h) {
         C.any_bc |= p.bc[f] != 0;
         C.any_pressure |= p.bc[f] == LBM_BC_PRESSURE;
         C.rho_bc[f] = (R)p.rho_bc[f];
+        C.rho_bc_dev[f] = (R)(p.rho_bc[f] - 1.0);
         for (int c = 0; c < 3; ++c) C.vel_bc[f][c] = (R)p.vel_bc[f][c];
     }
     C.bc_form = p.bc_form;
@@ -212,6 +215,7 @@ int sp_launch_steps(LbmHandle* h, int32_t n, bool macros_last) {
     case LBM_STORE_F32: return run_steps<LBM_STORE_F32>(h, n, macros_last);
     case LBM_STORE_F16_DEV: return run_steps<LBM_STORE_F16_DEV>(h, n, macros_last);
     case LBM_STORE_BF16_DEV: return run_steps<LBM_STORE_BF16_DEV>(h, n, macros_last);
+    case LBM_STORE_F32_DEV: return run_steps<LBM_STORE_F32_DEV>(h, n, macros_last);
     case LBM_STORE_F64: return run_steps<LBM_STORE_F64>(h, n, macros_last);
     }
     return lbm_set_err(h, LBM_EINVAL, "unknown storage");
@@ -224,6 +228,7 @@ int sp_launch_init(LbmHandle* h, const void* rho_nodes, const void* v_nodes) {
     case LBM_STORE_F32: return run_init<LBM_STORE_F32>(h, r, v);
     case LBM_STORE_F16_DEV: return run_init<LBM_STORE_F16_DEV>(h, r, v);
     case LBM_STORE_BF16_DEV: return run_init<LBM_STORE_BF16_DEV>(h, r, v);
+    case LBM_STORE_F32_DEV: return run_init<LBM_STORE_F32_DEV>(h, r, v);
     case LBM_STORE_F64: return run_init<LBM_STORE_F64>(h, r, v);
     }
     return lbm_set_err(h, LBM_EINVAL, "unknown storage");

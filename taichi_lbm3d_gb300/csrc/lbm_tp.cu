@@ -193,7 +193,8 @@ __device__ __forceinline__ void tp_collide_and_store(typename Codec<STORE>::R* F
                                                      const typename Codec<STORE>::R* __restrict__ psi,
                                                      typename Codec<STORE>::R rr, typename Codec<STORE>::R rb,
                                                      typename Codec<STORE>::T* __restrict__ fout,
-                                                     typename Codec<STORE>::R* __restrict__ cs_out) {
+                                                     typename Codec<STORE>::R* __restrict__ cs_out,
+                                                     float* __restrict__ rref_out) {
     using Cd = Codec<STORE>;
     using R = typename Cd::R;
     R Cx, Cy, Cz;
@@ -208,10 +209,7 @@ __device__ __forceinline__ void tp_collide_and_store(typename Codec<STORE>::R* F
     R sv, so;
     s_local<R>(T, psi[n], sv, so);
     collide_tp<R, FORCE>(F, r, vx, vy, vz, cc, n0, n1, n2, sv, so, T);
-    typename Cd::T* out = fout + lbm_eoff32(n);
-#define LBM_S(S) out[32 * S] = Cd::template enc<S>(F[S]);
-    LBM_S(0) LBM_ALL_DIRS(LBM_S)
-#undef LBM_S
+    store_node<STORE>(F, fout, n, r, rref_out);
     R cs[9];
     recolour_amounts<R>(rr, rb, vx, vy, vz, Cx, Cy, Cz, cc, cs);
     const int64_t np = T.sp.np;
@@ -308,7 +306,9 @@ __global__ void __launch_bounds__(256) tp_flow_kernel(const __grid_constant__ Tp
                                                       const typename Codec<STORE>::R* __restrict__ rr,
                                                       const typename Codec<STORE>::R* __restrict__ rb,
                                                       const typename Codec<STORE>::R* __restrict__ psi,
-                                                      typename Codec<STORE>::R* __restrict__ cs_out) {
+                                                      typename Codec<STORE>::R* __restrict__ cs_out,
+                                                      const float* __restrict__ rref_in,
+                                                      float* __restrict__ rref_out) {
     using Cd = Codec<STORE>;
     using R = typename Cd::R;
     const SpConsts<R>& C = T.sp;
@@ -318,25 +318,27 @@ __global__ void __launch_bounds__(256) tp_flow_kernel(const __grid_constant__ Tp
     const int i = lbm_pi(pc), j = lbm_pj(pc), k = lbm_pk(pc);
     const int64_t np = C.np;
     R F[19];
-    gather_node<STORE>(F, fin, map, n, C.nx, C.ny, C.nz, i, j, k);
-    if (C.any_bc && on_face(i, j, k, C, false)) apply_faces<R>(F, i, j, k, n, C, map, v);  // v = previous step's
+    gather_node<STORE>(F, fin, map, n, C.nx, C.ny, C.nz, i, j, k, rref_in);
+    if (C.any_bc && on_face(i, j, k, C, false)) apply_faces<R, Cd::DEV>(F, i, j, k, n, C, map, v);  // v: previous step
     R r = F[0];
 #pragma unroll
     for (int s = 1; s < 19; ++s) r = r + F[s];
+    const R rho = Cd::DEV ? (R)1 + r : r;
     R vx = vsum<0>(F), vy = vsum<1>(F), vz = vsum<2>(F);
-    vx = vx / r;
-    vy = vy / r;
-    vz = vz / r;
+    vx = vx / rho;
+    vy = vy / rho;
+    vz = vz / rho;
     if constexpr (FORCE) {
-        vx = vx + C.fhalf[0] / r;
-        vy = vy + C.fhalf[1] / r;
-        vz = vz + C.fhalf[2] / r;
+        vx = vx + C.fhalf[0] / rho;
+        vy = vy + C.fhalf[1] / rho;
+        vz = vz + C.fhalf[2] / rho;
     }
-    rho_out[n] = r;
+    rho_out[n] = rho;
     v[n] = vx;
     v[np + n] = vy;
     v[2 * np + n] = vz;
-    tp_collide_and_store<STORE, FORCE>(F, r, vx, vy, vz, n, i, j, k, T, map, psi, rr[n], rb[n], fout, cs_out);
+    tp_collide_and_store<STORE, FORCE>(F, r, vx, vy, vz, n, i, j, k, T, map, psi, rr[n], rb[n], fout, cs_out,
+                                       rref_out);
 }
 
 // Initial state (TP:174-187) and the first collision: rho = 1, v = 0, F = feq(1, 0),
@@ -347,8 +349,9 @@ __global__ void tp_init_kernel(const __grid_constant__ TpConsts<typename Codec<S
                                const uint32_t* __restrict__ coord, typename Codec<STORE>::R* __restrict__ v,
                                typename Codec<STORE>::R* __restrict__ rho_out, typename Codec<STORE>::R* __restrict__ rr,
                                typename Codec<STORE>::R* __restrict__ rb, const typename Codec<STORE>::R* __restrict__ psi,
-                               typename Codec<STORE>::R* __restrict__ cs_out) {
-    using R = typename Codec<STORE>::R;
+                               typename Codec<STORE>::R* __restrict__ cs_out, float* __restrict__ rref_out) {
+    using Cd = Codec<STORE>;
+    using R = typename Cd::R;
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= T.sp.n_fluid) return;
     const uint32_t pc = __ldg(coord + n);
@@ -362,9 +365,10 @@ __global__ void tp_init_kernel(const __grid_constant__ TpConsts<typename Codec<S
     v[2 * np + n] = (R)0;
     rho_out[n] = (R)1.0;
     R F[19];
-    lbm_feq_all<R>((R)1.0, (R)0, (R)0, (R)0, F);
-    tp_collide_and_store<STORE, FORCE>(F, (R)1.0, (R)0, (R)0, (R)0, n, lbm_pi(pc), lbm_pj(pc), lbm_pk(pc), T, map, psi,
-                                       r0, b0, fout, cs_out);
+    if constexpr (Cd::DEV) lbm_feq_dev_all<R>((R)0, (R)0, (R)0, (R)0, F);
+    else lbm_feq_all<R>((R)1.0, (R)0, (R)0, (R)0, F);
+    tp_collide_and_store<STORE, FORCE>(F, Cd::DEV ? (R)0 : (R)1.0, (R)0, (R)0, (R)0, n, lbm_pi(pc), lbm_pj(pc),
+                                       lbm_pk(pc), T, map, psi, r0, b0, fout, cs_out, rref_out);
 }
 
 template <typename R>
@@ -408,7 +412,8 @@ int tp_init_t(LbmHandle* h) {
     const int grid = (int)((h->n_fluid + h->block - 1) / h->block);
     auto k = h->force ? tp_init_kernel<STORE, true> : tp_init_kernel<STORE, false>;
     k<<<grid, h->block, 0, h->stream>>>(T, (Tt*)h->d_f[0], h->d_map, h->d_coord, (R*)h->d_v, (R*)h->d_rho,
-                                        (R*)h->d_rr[0], (R*)h->d_rb[0], (const R*)h->d_psi, (R*)h->d_cs);
+                                        (R*)h->d_rr[0], (R*)h->d_rb[0], (const R*)h->d_psi, (R*)h->d_cs,
+                                        h->d_rref[0]);
     rc = lbm_cuda_check(h, cudaGetLastError(), "tp_init_kernel launch");
     if (!rc) rc = lbm_cuda_check(h, cudaStreamSynchronize(h->stream), "tp_init");
     return rc;
@@ -431,7 +436,8 @@ int tp_steps_t(LbmHandle* h, int32_t nsteps) {
         h->ccur ^= 1;
         kb<<<grid, h->block, 0, h->stream>>>(T, (const Tt*)h->d_f[h->cur], (Tt*)h->d_f[h->cur ^ 1], h->d_map, h->d_coord,
                                              (R*)h->d_v, (R*)h->d_rho, (const R*)h->d_rr[h->ccur],
-                                             (const R*)h->d_rb[h->ccur], (const R*)h->d_psi, (R*)h->d_cs);
+                                             (const R*)h->d_rb[h->ccur], (const R*)h->d_psi, (R*)h->d_cs,
+                                             h->d_rref[h->cur], h->d_rref[h->cur ^ 1]);
         rc = lbm_cuda_check(h, cudaGetLastError(), "tp_flow_kernel launch");
         if (rc) return rc;
         h->cur ^= 1;
@@ -446,6 +452,7 @@ int tp_launch_init(LbmHandle* h) {
     case LBM_STORE_F32: return tp_init_t<LBM_STORE_F32>(h);
     case LBM_STORE_F16_DEV: return tp_init_t<LBM_STORE_F16_DEV>(h);
     case LBM_STORE_BF16_DEV: return tp_init_t<LBM_STORE_BF16_DEV>(h);
+    case LBM_STORE_F32_DEV: return tp_init_t<LBM_STORE_F32_DEV>(h);
     case LBM_STORE_F64: return tp_init_t<LBM_STORE_F64>(h);
     }
     return lbm_set_err(h, LBM_EINVAL, "unknown storage");
@@ -456,6 +463,7 @@ int tp_launch_steps(LbmHandle* h, int32_t n, bool) {
     case LBM_STORE_F32: return tp_steps_t<LBM_STORE_F32>(h, n);
     case LBM_STORE_F16_DEV: return tp_steps_t<LBM_STORE_F16_DEV>(h, n);
     case LBM_STORE_BF16_DEV: return tp_steps_t<LBM_STORE_BF16_DEV>(h, n);
+    case LBM_STORE_F32_DEV: return tp_steps_t<LBM_STORE_F32_DEV>(h, n);
     case LBM_STORE_F64: return tp_steps_t<LBM_STORE_F64>(h, n);
     }
     return lbm_set_err(h, LBM_EINVAL, "unknown storage");

@@ -158,21 +158,29 @@ class LB3D_Solver_Single_Phase:
 
     def permeability(self, axis=0):
         """Permeability along ``axis`` from the Darcy velocity (mean v over all
-        cells, solid cells count as 0):  k = nu_eff <v> / F_eff  for a body force,
+        cells, solid cells count as 0):  k = nu_eff <v> / F_eff  for a body force
+        (F_eff = the momentum the Guo term injects per step: F/9 in the class
+        form, :236; F/3 in the script form; F in the standard form),
         k = nu_eff <v> (L-1) / ((rho_in - rho_out)/3)  for a pressure drop."""
         st = self.stats()
-        ncell = self.nx * self.ny * self.nz
-        vmean = st.mom[axis] / ncell
+        return self._k_from_darcy(st.mom[axis] / (self.nx * self.ny * self.nz), axis)
+
+    def _k_from_darcy(self, vmean, axis):
         f = (self.fx, self.fy, self.fz)[axis]
         if f != 0:
-            # momentum the Guo term injects per step: F/9 (class, :236), F/3
-            # (script form), F (standard form)
             f_eff = f * {"class": 1.0 / 9.0, "script": 1.0 / 3.0, "standard": 1.0}[self.guo_convention]
             return self.nu_eff() * vmean / f_eff
         rin = (self.rho_bcxl, self.rho_bcyl, self.rho_bczl)[axis]
         rout = (self.rho_bcxr, self.rho_bcyr, self.rho_bczr)[axis]
         L = (self.nx, self.ny, self.nz)[axis]
         return self.nu_eff() * vmean * (L - 1) / ((rin - rout) / 3.0)
+
+    def run_to_convergence(self, tol=1e-6, check_every=500, max_steps=1_000_000, axis=0):
+        """Step until the permeability changes by <= tol (relative) over
+        ``check_every`` steps; returns dict(k, darcy_v, steps, converged)."""
+        dv, steps, conv = self._need().run_to_convergence(tol, check_every, max_steps, axis)
+        self._cache = None
+        return {"k": self._k_from_darcy(dv, axis), "darcy_v": dv, "steps": steps, "converged": conv}
 
     def export_VTK(self, n):
         rho, v = self._macros()

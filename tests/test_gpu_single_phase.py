@@ -189,7 +189,7 @@ def test_reductions_match_host_sums():
 # Transient (300 steps from rest) error of the deviation-storage variants,
 # normwise against the FP64 oracle: FP16 keeps 11 significant bits of f - w,
 # BF16 8; FP64 must agree to round-off.
-@pytest.mark.parametrize("storage,tol", [("f64", 1e-9), ("f16", 2e-2), ("bf16", 1e-1)])
+@pytest.mark.parametrize("storage,tol", [("f64", 1e-9), ("f32dev", 1e-4), ("f16", 2e-2), ("bf16", 1e-1)])
 def test_storage_variants_close_to_fp64_oracle(storage, tol):
     solid = sphere_pack((32, 24, 24), 2.5, 5, 0.45, seed=9)
     p = oracle_params((32, 24, 24), niu=0.1, bc=(1, 1, 0, 0, 0, 0), rho_bc=(1.002, 1.0, 1, 1, 1, 1),
@@ -203,6 +203,7 @@ def test_storage_variants_close_to_fp64_oracle(storage, tol):
     # velocities are ~1e-4: compare the deviation from rest of rho, and v normwise
     e_rho = np.abs(rho[fl] - o.field("rho")[fl]).max() / np.abs(o.field("rho")[fl] - 1.0).max()
     e_v = G.normwise_rel(v, o.field("v"), fl)
+    print("storage %s: e_rho %.3e e_v %.3e" % (storage, e_rho, e_v))
     assert e_rho < tol and e_v < tol, (storage, e_rho, e_v)
 
 
