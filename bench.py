@@ -228,6 +228,77 @@ def convergence(storages=("f64", "f32", "f32dev", "f16", "bf16"), tol=1e-6, chec
     return out
 
 
+def batched(n_sub=256, seeds0=4000, fp64_subset=16, storage="f16", tol=1e-6, check_every=500,
+            max_steps=100_000, log=lambda m: print(m, file=sys.stderr, flush=True)):
+    """Config 4: n_sub seeded subvolumes (edges {48..160}, r U[3,8], phi
+    U[0.25,0.5]), fx = 1e-6, periodic, niu 0.1, each to steady state:
+    one persistent graph-captured batch (autotuned) against a serial loop of the
+    plain FP32 kernel; per-sample k error against FP64 on a subset."""
+    from taichi_lbm3d_gb300 import autotune
+    from taichi_lbm3d_gb300.batch import Batch, config4_solids
+    t0 = time.perf_counter()
+    solids = config4_solids(range(seeds0, seeds0 + n_sub))          # spawned pool, before CUDA
+    log("generated %d subvolumes in %.1f s" % (n_sub, time.perf_counter() - t0))
+    edges = [s.shape[0] for s in solids]
+    by_edge = {}
+    for s in solids:
+        by_edge.setdefault(s.shape[0], [])
+        if len(by_edge[s.shape[0]]) < 4:
+            by_edge[s.shape[0]].append(s)
+    tuned = autotune.tune(by_edge, storage=storage, log=log)
+    tiles, block = autotune.plan(edges, tuned)
+    force = (1e-6, 0.0, 0.0)
+
+    def run_batch(subset, sto, tl, blk):
+        b = Batch([solids[q] for q in subset], niu=NIU, force=force, storage=sto)
+        b.configure([tl[q] for q in subset], blk)
+        b.init()
+        t = time.perf_counter()
+        d, st, cv = b.run_to_convergence(tol=tol, check_every=check_every, max_steps=max_steps)
+        secs = time.perf_counter() - t
+        k = b.permeability(d)
+        nf = b.info()["n_fluid"]
+        b.close()
+        return k, st, cv, secs, nf
+
+    allq = list(range(n_sub))
+    k_b, st_b, cv_b, secs_b, nf_all = run_batch(allq, storage, tiles, block)
+    log("batched %s: %.1f s, %d/%d converged" % (storage, secs_b, cv_b.sum(), n_sub))
+    # serial loop of the plain FP32 kernel, one lattice at a time
+    from taichi_lbm3d_gb300 import LB3D_Solver_Single_Phase
+    t = time.perf_counter()
+    k_s, st_s = [], []
+    for q in allq:
+        lb = LB3D_Solver_Single_Phase(*solids[q].shape, storage="f32", viscosity_convention="standard",
+                                      guo_convention="standard")
+        lb.solid.from_numpy(solids[q])
+        lb.set_viscosity(NIU)
+        lb.set_force(force)
+        lb.init_simulation()
+        r = lb.run_to_convergence(tol=tol, check_every=check_every, max_steps=max_steps)
+        lb.close()
+        k_s.append(r["k"])
+        st_s.append(r["steps"])
+    secs_s = time.perf_counter() - t
+    log("serial f32: %.1f s" % secs_s)
+    sub = allq[:fp64_subset]
+    k64, _, cv64, secs64, _ = run_batch(sub, "f64", [256] * n_sub, 128)
+    err_b = np.abs(k_b[sub] - k64) / np.abs(k64)
+    err_s = np.abs(np.array(k_s)[sub] - k64) / np.abs(k64)
+    total_updates = float(np.sum([int((s == 0).sum()) * n for s, n in zip(solids, st_b)]))
+    return {"n_sub": n_sub, "edges": {str(e): edges.count(e) for e in sorted(set(edges))},
+            "n_fluid_total": int(nf_all), "storage": storage, "block": block,
+            "tiles": {str(e): int(tuned[e]["tile"]) for e in sorted(tuned)},
+            "batched_seconds": secs_b, "batched_mlups": total_updates / secs_b / 1e6,
+            "batched_converged": int(cv_b.sum()), "serial_f32_seconds": secs_s,
+            "wall_time_ratio_serial_over_batched": secs_s / secs_b,
+            "steps_batched_mean": float(np.mean(st_b)), "steps_serial_mean": float(np.mean(st_s)),
+            "fp64_subset": len(sub), "fp64_seconds": secs64, "fp64_converged": int(cv64.sum()),
+            "k_rel_err_batched_vs_f64_max": float(err_b.max()), "k_rel_err_batched_vs_f64_median": float(np.median(err_b)),
+            "k_rel_err_serial_f32_vs_f64_max": float(err_s.max()),
+            "k_rel_err_serial_f32_vs_f64_median": float(np.median(err_s))}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -238,7 +309,14 @@ def main():
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--convergence", action="store_true",
                     help="run the 256^3 pack to steady state in FP64/FP32/FP16/BF16 and print k errors")
+    ap.add_argument("--batched", action="store_true",
+                    help="config 4: batched persistent launch vs serial plain kernel, k error vs FP64")
+    ap.add_argument("--n-sub", type=int, default=256)
     a = ap.parse_args()
+    if a.batched:
+        res = batched(n_sub=a.n_sub)
+        print(json.dumps({"batched": res}))
+        return 0
     if a.convergence:
         res = convergence()
         print(json.dumps({"convergence": res, "config": workload_config(), "tol": 1e-6, "check_every": 500,

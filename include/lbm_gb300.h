@@ -177,6 +177,32 @@ int lbm_set_populations(LbmHandle* h, const double* f);
  * boundary condition (streaming1, SP:259-269): in/out [19][n_fluid] FP32. */
 int lbm_debug_stream(LbmHandle* h, const float* f_in, float* f_out);
 
+/* ------------------------------------------------------------------ batches
+ * Many independent porous subvolumes (no counterpart in the reference, which
+ * runs one lattice per process): all faces periodic, shared parameters, one
+ * persistent kernel per time step over all active subvolumes, check_every
+ * steps captured in one CUDA graph.  dims: [n_sub][3]; solids: the n_sub
+ * x-fastest masks back to back. */
+typedef struct LbmBatch LbmBatch;
+int lbm_batch_create(const LbmParams* params, int32_t n_sub, const int32_t* dims, const int8_t* solids,
+                     LbmBatch** out);
+int lbm_batch_destroy(LbmBatch* b);
+/* Work-tile length in nodes per subvolume and CTA size of the persistent kernel
+ * (chosen by the autotuner in taichi_lbm3d_gb300/autotune.py). */
+int lbm_batch_configure(LbmBatch* b, const int32_t* tile_len, int32_t block);
+/* Rest state f = feq(1, 0) in every subvolume, all subvolumes active. */
+int lbm_batch_init(LbmBatch* b);
+/* nsteps steps of the active subvolumes, in graph launches of `chunk` steps
+ * (use_graph = 1) or plain launches (0). */
+int lbm_batch_step(LbmBatch* b, int32_t nsteps, int32_t chunk, int32_t use_graph);
+/* Run until each subvolume's FP64 Darcy velocity along x changes by <= tol
+ * between checks; converged subvolumes drop out of the work list.  Per
+ * subvolume outputs: Darcy velocity, steps taken, converged flag. */
+int lbm_batch_run_to_convergence(LbmBatch* b, double tol, int32_t check_every, int64_t max_steps, int32_t use_graph,
+                                 double* darcy, int64_t* steps, int32_t* converged);
+int lbm_batch_get_stream(LbmBatch* b, void** stream);
+int lbm_batch_info(LbmBatch* b, int64_t* n_nodes, int64_t* n_fluid, int32_t* grid, int32_t* n_tiles);
+
 /* Copy the message of the last error on this handle (or the last global error
  * when h is NULL) into buf. */
 int lbm_last_error(LbmHandle* h, char* buf, size_t n);

@@ -1,0 +1,62 @@
+"""Batched persistent launch (K5) and its autotuner."""
+import json
+
+import numpy as np
+import pytest
+
+from taichi_lbm3d_gb300 import _native
+from taichi_lbm3d_gb300.geometry import sphere_pack
+
+pytestmark = pytest.mark.gpu
+
+
+def solids():
+    return [sphere_pack((24, 24, 24), 2, 4, 0.45, seed=51), sphere_pack((32, 32, 32), 2.5, 5, 0.40, seed=52),
+            sphere_pack((16, 16, 16), 1.5, 3, 0.50, seed=53)]
+
+
+@pytest.mark.parametrize("storage", ["f32", "f16"])
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_batch_matches_single_lattices(storage, use_graph):
+    from taichi_lbm3d_gb300.batch import Batch
+    S = solids()
+    b = Batch(S, niu=0.1, force=(1e-5, 0, 0), storage=storage)
+    b.configure([64, 128, 32], 128)
+    b.init()
+    darcy, steps, conv = b.run_to_convergence(tol=0.0, check_every=50, max_steps=100, use_graph=use_graph)
+    assert list(steps) == [100, 100, 100] and not conv.any()
+    for q, s in enumerate(S):
+        lat = _native.Lattice(_native.make_params(s.shape, niu=0.1, force=(1e-5, 0, 0), visc_convention=1,
+                                                  guo_convention=2, storage=storage))
+        lat.set_geometry(s)
+        lat.init()
+        lat.step(100)
+        ref = lat.stats().mom[0] / s.size
+        assert abs(darcy[q] - ref) <= 1e-12 * abs(ref), (q, darcy[q], ref)
+    b.close()
+
+
+def test_batch_converges_and_drops_subvolumes():
+    from taichi_lbm3d_gb300.batch import Batch
+    S = solids()
+    b = Batch(S, niu=0.1, force=(1e-5, 0, 0), storage="f32dev")
+    b.configure([256] * 3, 256)
+    b.init()
+    darcy, steps, conv = b.run_to_convergence(tol=1e-4, check_every=100, max_steps=20000)
+    assert conv.all() and (steps > 0).all()
+    k = b.permeability(darcy)
+    assert (k > 0).all() and np.isfinite(k).all()
+
+
+def test_autotuner_caches(tmp_path):
+    from taichi_lbm3d_gb300 import autotune
+    path = str(tmp_path / "tune.json")
+    S = solids()
+    res = autotune.tune({24: [S[0]], 16: [S[2]]}, storage="f32", path=path)
+    assert set(res) == {16, 24} and all(r["tile"] in autotune.TILES for r in res.values())
+    data = json.load(open(path))
+    assert len(data) == 2
+    res2 = autotune.tune({24: [S[0]], 16: [S[2]]}, storage="f32", path=path)
+    assert res2[24]["when"] == res[24]["when"]          # served from the cache
+    tiles, block = autotune.plan([24, 16, 24], res)
+    assert len(tiles) == 3 and block in autotune.BLOCKS
