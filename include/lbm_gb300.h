@@ -200,6 +200,9 @@ int lbm_batch_step(LbmBatch* b, int32_t nsteps, int32_t chunk, int32_t use_graph
  * subvolume outputs: Darcy velocity, steps taken, converged flag. */
 int lbm_batch_run_to_convergence(LbmBatch* b, double tol, int32_t check_every, int64_t max_steps, int32_t use_graph,
                                  double* darcy, int64_t* steps, int32_t* converged);
+/* rho and v (dense, x fastest, solid cells 1 and 0) of subvolume `sub` from its
+ * current populations: e.g. the converged field of a training sample. */
+int lbm_batch_get_macros(LbmBatch* b, int32_t sub, float* rho, float* v);
 int lbm_batch_get_stream(LbmBatch* b, void** stream);
 int lbm_batch_info(LbmBatch* b, int64_t* n_nodes, int64_t* n_fluid, int32_t* grid, int32_t* n_tiles);
 

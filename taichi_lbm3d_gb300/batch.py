@@ -25,6 +25,7 @@ _SIGS = {
     "lbm_batch_run_to_convergence": [_P, ctypes.c_double, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32, _P, _P,
                                      _P],
     "lbm_batch_get_stream": [_P, ctypes.POINTER(_P)],
+    "lbm_batch_get_macros": [_P, ctypes.c_int32, _P, _P],
     "lbm_batch_info": [_P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
                        ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)],
 }
@@ -95,6 +96,15 @@ class Batch:
                                                     1 if use_graph else 0, _native.ptr(d), _native.ptr(st),
                                                     _native.ptr(cv)))
         return d, st, cv.astype(bool)
+
+    def macros(self, q):
+        """Dense rho (nx,ny,nz) and v (nx,ny,nz,3) of subvolume q from its current state."""
+        shape = self.shapes[q]
+        nc = int(np.prod(shape))
+        rho = np.empty(nc, np.float32)
+        v = np.empty(nc * 3, np.float32)
+        self._c(_lib().lbm_batch_get_macros(self.h, int(q), _native.ptr(rho), _native.ptr(v)))
+        return rho.reshape(shape, order="F"), v.reshape((nc, 3)).reshape(shape + (3,), order="F")
 
     def stream(self):
         s = _P()

@@ -113,6 +113,37 @@ __global__ void __launch_bounds__(256) batch_step_kernel(const __grid_constant__
     }
 }
 
+// rho and v of one subvolume's nodes from its current populations (the
+// macroscopic step of the next update, without collision or store).
+template <int STORE, bool FORCE>
+__global__ void batch_macros_kernel(const __grid_constant__ SpConsts<typename Codec<STORE>::R> C, BatchSub sd,
+                                    const typename Codec<STORE>::T* __restrict__ fin, const int32_t* __restrict__ map,
+                                    const uint32_t* __restrict__ coord, const float* __restrict__ rref_in,
+                                    float* __restrict__ out) {
+    using Cd = Codec<STORE>;
+    using R = typename Cd::R;
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= sd.n_fluid) return;
+    const int n = sd.node_begin + a;
+    const uint32_t pc = __ldg(coord + n);
+    R F[19];
+    gather_node<STORE>(F, fin, map + sd.map_off, n, sd.nx, sd.ny, sd.nz, lbm_pi(pc), lbm_pj(pc), lbm_pk(pc), rref_in);
+    R r = F[0];
+#pragma unroll
+    for (int s = 1; s < 19; ++s) r = r + F[s];
+    const R rho = Cd::DEV ? (R)1 + r : r;
+    R vx = vsum<0>(F) / rho, vy = vsum<1>(F) / rho, vz = vsum<2>(F) / rho;
+    if constexpr (FORCE) {
+        vx = vx + C.fhalf[0] / rho;
+        vy = vy + C.fhalf[1] / rho;
+        vz = vz + C.fhalf[2] / rho;
+    }
+    out[4 * a] = (float)rho;
+    out[4 * a + 1] = (float)vx;
+    out[4 * a + 2] = (float)vy;
+    out[4 * a + 3] = (float)vz;
+}
+
 template <int STORE, bool FORCE>
 __global__ void batch_init_kernel(const __grid_constant__ SpConsts<typename Codec<STORE>::R> C,
                                   typename Codec<STORE>::T* __restrict__ fout, const BatchSub* __restrict__ subs,
@@ -199,6 +230,20 @@ int init_t(LbmBatch* b) {
     auto k = h->force ? batch_init_kernel<STORE, true> : batch_init_kernel<STORE, false>;
     k<<<grid, 256, 0, h->stream>>>(C, (typename Cd::T*)h->d_f[0], b->d_subs, (int)b->subs.size(), h->d_rref[0]);
     return lbm_cuda_check(h, cudaGetLastError(), "batch_init_kernel launch");
+}
+
+template <int STORE>
+int macros_t(LbmBatch* b, int q, float* d_out) {
+    using Cd = Codec<STORE>;
+    using R = typename Cd::R;
+    LbmHandle* h = &b->h;
+    const SpConsts<R> C = sp_make_consts<R>(h);
+    const BatchSub sd = b->subs[q];
+    const int grid = (sd.n_fluid + 255) / 256;
+    auto k = h->force ? batch_macros_kernel<STORE, true> : batch_macros_kernel<STORE, false>;
+    if (grid > 0)
+        k<<<grid, 256, 0, h->stream>>>(C, sd, (const typename Cd::T*)h->d_f[0], h->d_map, h->d_coord, h->d_rref[0], d_out);
+    return lbm_cuda_check(h, cudaGetLastError(), "batch_macros_kernel launch");
 }
 
 int rebuild_tiles(LbmBatch* b) {
@@ -493,6 +538,48 @@ int lbm_batch_run_to_convergence(LbmBatch* b, double tol, int32_t check_every, i
     for (size_t q = 0; q < ns; ++q) {
         darcy[q] = cur[q];
         steps[q] = b->steps[q];
+    }
+    return LBM_OK;
+}
+
+int lbm_batch_get_macros(LbmBatch* b, int32_t sub, float* rho, float* v) {
+    if (!b || !rho || !v) return lbm_set_err(nullptr, LBM_EINVAL, "lbm_batch_get_macros: NULL");
+    if (sub < 0 || sub >= (int32_t)b->subs.size()) return batch_err(b, LBM_EINVAL, "lbm_batch_get_macros: bad subvolume");
+    LbmHandle* h = &b->h;
+    cudaSetDevice(h->device);
+    const BatchSub sd = b->subs[sub];
+    float* d_out = nullptr;
+    if (cudaMalloc((void**)&d_out, sizeof(float) * 4 * std::max(1, sd.n_fluid)) != cudaSuccess)
+        return batch_err(b, LBM_ENOMEM, "lbm_batch_get_macros: out of device memory");
+    int rc = 0;
+    switch (h->p.storage) {
+    case LBM_STORE_F32: rc = macros_t<LBM_STORE_F32>(b, sub, d_out); break;
+    case LBM_STORE_F16_DEV: rc = macros_t<LBM_STORE_F16_DEV>(b, sub, d_out); break;
+    case LBM_STORE_BF16_DEV: rc = macros_t<LBM_STORE_BF16_DEV>(b, sub, d_out); break;
+    case LBM_STORE_F32_DEV: rc = macros_t<LBM_STORE_F32_DEV>(b, sub, d_out); break;
+    case LBM_STORE_F64: rc = macros_t<LBM_STORE_F64>(b, sub, d_out); break;
+    }
+    std::vector<float> tmp(4 * (size_t)sd.n_fluid);
+    if (!rc && sd.n_fluid)
+        rc = lbm_cuda_check(h, cudaMemcpyAsync(tmp.data(), d_out, sizeof(float) * tmp.size(), cudaMemcpyDeviceToHost, h->stream), "copy macros");
+    if (!rc) rc = lbm_cuda_check(h, cudaStreamSynchronize(h->stream), "batch macros");
+    cudaFree(d_out);
+    if (rc) return rc;
+    // scatter to the dense lattice (solid: rho = 1, v = 0) through the host copy of the map
+    const int64_t nc = (int64_t)sd.nx * sd.ny * sd.nz;
+    std::vector<int32_t> map(nc);
+    rc = lbm_cuda_check(h, cudaMemcpy(map.data(), h->d_map + sd.map_off, sizeof(int32_t) * nc, cudaMemcpyDeviceToHost), "copy map");
+    if (rc) return rc;
+    for (int64_t c = 0; c < nc; ++c) {
+        const int32_t nd = map[c];
+        if (nd < 0) {
+            rho[c] = 1.0f;
+            v[3 * c] = v[3 * c + 1] = v[3 * c + 2] = 0.0f;
+        } else {
+            const int64_t a = nd - sd.node_begin;
+            rho[c] = tmp[4 * a];
+            for (int d = 0; d < 3; ++d) v[3 * c + d] = tmp[4 * a + 1 + d];
+        }
     }
     return LBM_OK;
 }
