@@ -126,6 +126,15 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def max_over_ranks(secs, device="cpu"):
+    """Slowest rank's time: every replica does the same work, the job ends with the last."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(secs)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def time_device(lat, steps, warmup):
     """Warm up, then time `steps` launches with CUDA events on the library stream."""
     import torch
@@ -299,6 +308,73 @@ def batched(n_sub=256, seeds0=4000, fp64_subset=16, storage="f16", tol=1e-6, che
             "k_rel_err_serial_f32_vs_f64_median": float(np.median(err_s))}
 
 
+def two_phase(steps=20000, every=500, shape=(131, 131, 131), storages=("f64", "f32", "f16"),
+              log=lambda m: print(m, file=sys.stderr, flush=True)):
+    """Config 3: colour-gradient drainage on a 131^3 pack (seed 3, r U[3,8],
+    phi 0.40), psi = -1 with a 5-node psi = +1 slab at x-left, constant psi +1 /
+    -1 and pressure 1.001 / 1.0 on the x faces, periodic y/z, CapA 0.005,
+    psi_solid 0.7, niu_l 0.05, niu_g 0.2.  Saturation and interface position
+    every `every` steps for each storage, compared with FP64; MLUPS timed with
+    CUDA events on a separate 2000-step run."""
+    import torch
+    from taichi_lbm3d_gb300 import LB3D_Solver_Two_Phase
+    from taichi_lbm3d_gb300.geometry import sphere_pack
+    solid = sphere_pack(shape, 3.0, 8.0, 0.40, seed=3)
+    psi0 = -np.ones(shape, np.float32)
+    psi0[:5] = 1.0
+
+    def make(sto):
+        s = LB3D_Solver_Two_Phase(*shape, storage=sto)
+        s.fx = 0.0
+        s.niu_l, s.niu_g, s.psi_solid, s.CapA = 0.05, 0.2, 0.7, 0.005
+        s.bc_x_left, s.rho_bcxl, s.bc_x_right, s.rho_bcxr = 1, 1.001, 1, 1.0
+        s.bc_psi_x_left, s.psi_x_left, s.bc_psi_x_right, s.psi_x_right = 1, 1.0, 1, -1.0
+        s.solid.from_numpy(solid)
+        s.psi.from_numpy(psi0)
+        s.init_simulation()
+        return s
+
+    out = {"n_fluid": int((solid == 0).sum()), "steps": steps, "every": every}
+    curves = {}
+    for sto in storages:
+        s = make(sto)
+        sat, pos = [], []
+        t = time.perf_counter()
+        for _ in range(steps // every):
+            s.run(every)
+            sat.append(s.saturation())
+            pos.append(s.interface_position())
+        curves[sto] = (np.array(sat), np.array(pos))
+        log("two-phase %s: %d steps in %.1f s, final S %.4f" % (sto, steps, time.perf_counter() - t, sat[-1]))
+        s.close()
+        if sto != "f64":
+            s = make(sto)
+            lat = s._lat
+            nsteps = 2000
+            stream = torch.cuda.ExternalStream(lat.stream())
+            lat.step_async(20)
+            lat.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            lat.step_async(nsteps)
+            e1.record(stream)
+            e1.synchronize()
+            secs = e0.elapsed_time(e1) / 1e3
+            out["mlups_" + sto] = out["n_fluid"] * nsteps / secs / 1e6
+            out["gbs_algorithmic_" + sto] = {"f32": 176, "f16": 100}[sto] * out["n_fluid"] * nsteps / secs / 1e9
+            s.close()
+    s64, p64 = curves["f64"]
+    for sto in storages:
+        if sto == "f64":
+            continue
+        sa, pa = curves[sto]
+        out["saturation_max_abs_err_" + sto] = float(np.abs(sa - s64).max())
+        out["interface_max_abs_err_" + sto] = float(np.nanmax(np.abs(pa - p64)))
+    out["saturation_f64"] = [float(x) for x in s64]
+    out["interface_f64"] = [float(x) for x in p64]
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -312,7 +388,11 @@ def main():
     ap.add_argument("--batched", action="store_true",
                     help="config 4: batched persistent launch vs serial plain kernel, k error vs FP64")
     ap.add_argument("--n-sub", type=int, default=256)
+    ap.add_argument("--two-phase", action="store_true", help="config 3: two-phase drainage vs FP64")
     a = ap.parse_args()
+    if a.two_phase:
+        print(json.dumps({"two_phase": two_phase()}))
+        return 0
     if a.batched:
         res = batched(n_sub=a.n_sub)
         print(json.dumps({"batched": res}))
@@ -381,9 +461,7 @@ def main():
     st = lat.stats()
     lat.close()
     if world > 1:
-        t = torch.tensor([secs], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        secs = float(t.item())
+        secs = max_over_ranks(secs, "cuda")
         torch.distributed.barrier()
     clocks.stop()
     clk = clocks.summary(t_wall0, t_wall1)

@@ -55,7 +55,7 @@ namespace {
 using namespace lbmk;
 
 template <int STORE, bool FORCE, bool CHECK>
-__global__ void __launch_bounds__(256) batch_step_kernel(const __grid_constant__ SpConsts<typename Codec<STORE>::R> C,
+__global__ void __launch_bounds__(256, STORE == LBM_STORE_F64 ? 1 : 4) batch_step_kernel(const __grid_constant__ SpConsts<typename Codec<STORE>::R> C,
                                                          const BatchSub* __restrict__ subs,
                                                          const BatchTile* __restrict__ tiles,
                                                          const int32_t* __restrict__ n_tiles, int32_t* counter,

@@ -1,0 +1,89 @@
+"""Host-side logic that needs no GPU: I/O formats, synthetic geometry,
+autotuner planning, multi-rank timing reduction (gloo, world size 2)."""
+import os
+import socket
+
+import numpy as np
+import pytest
+
+from taichi_lbm3d_gb300 import autotune, geometry, vtk
+
+
+def test_vtk_roundtrip(tmp_path):
+    rng = np.random.default_rng(0)
+    shape = (5, 4, 3)
+    solid = (rng.random(shape) > 0.7).astype(np.int8)
+    rho = rng.random(shape).astype(np.float32)
+    v = rng.random(shape + (3,)).astype(np.float32)
+    f = vtk.grid_to_vtk(str(tmp_path / "out"), np.arange(5.0), np.arange(4.0), np.arange(3.0),
+                        {"Solid": solid, "rho": rho, "velocity": (v[..., 0], v[..., 1], v[..., 2])})
+    d = vtk.read_vtr(f)
+    assert np.array_equal(d["Solid"], solid) and np.array_equal(d["rho"], rho)
+    assert np.array_equal(d["velocity"], v)
+
+
+def test_ascii_geometry_roundtrip(tmp_path):
+    s = geometry.cavity_shell(6)
+    path = str(tmp_path / "geo.dat")
+    geometry.write_ascii_geometry(path, s)
+    assert np.array_equal(geometry.read_ascii_geometry(path, s.shape), s)
+    lines = open(path).read().split()
+    assert len(lines) == s.size and lines[0] == "1"          # x fastest, first cell is the shell
+
+
+def test_ascii_geometry_rejects_wrong_size(tmp_path):
+    path = str(tmp_path / "g.dat")
+    np.savetxt(path, np.zeros(10), fmt="%d")
+    with pytest.raises(ValueError):
+        geometry.read_ascii_geometry(path, (3, 3, 3))
+
+
+def test_sphere_pack_porosity_and_percolation():
+    from scipy import ndimage
+    s = geometry.sphere_pack((48, 40, 40), 3, 6, 0.4, seed=7)
+    s2 = geometry.sphere_pack((48, 40, 40), 3, 6, 0.4, seed=7)
+    assert np.array_equal(s, s2)                                # seeded, deterministic
+    raw = geometry.sphere_pack((48, 40, 40), 3, 6, 0.4, seed=7, percolate=False)
+    assert 1.0 - raw.mean() <= 0.4 + 1e-9                       # stopped at the target porosity
+    assert np.all(s >= raw)                                     # percolation only adds solid
+    fluid = s == 0
+    lab, _ = ndimage.label(np.concatenate([fluid, fluid], axis=1))   # y wrap by tiling
+    assert fluid[0].any() and fluid[-1].any()
+
+
+def test_distance_to_solid():
+    s = np.zeros((9, 9, 9), np.int8)
+    s[4, 4, 4] = 1
+    d = geometry.distance_to_solid(s)
+    assert d[4, 4, 4] == 0 and d[4, 4, 7] == 3 and abs(d[5, 5, 5] - np.sqrt(3)) < 1e-6
+
+
+def test_autotune_plan_uses_tuned_tiles():
+    tuned = {48: {"tile": 256, "block": 128}, 160: {"tile": 1024, "block": 256}}
+    tiles, block = autotune.plan([48, 48, 160], tuned)
+    assert tiles == [256, 256, 1024] and block == 256          # the 160^3 class holds most cells
+
+
+def _rank_main(rank, world, port, q):
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    import bench
+    q.put((rank, bench.max_over_ranks(1.0 + rank)))
+    dist.destroy_process_group()
+
+
+def test_max_over_ranks_gloo_world2():
+    import multiprocessing as mp
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    ps = [ctx.Process(target=_rank_main, args=(r, 2, port, q)) for r in range(2)]
+    for p in ps:
+        p.start()
+    got = dict(q.get(timeout=120) for _ in ps)
+    for p in ps:
+        p.join(timeout=60)
+    assert got == {0: 2.0, 1: 2.0}
