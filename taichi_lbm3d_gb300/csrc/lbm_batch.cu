@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(256, STORE == LBM_STORE_F64 ? 1 : 4) batch_ste
                 vz = vz + C.fhalf[2] / rho;
             }
             if constexpr (CHECK) acc += (double)vx;
-            collide_sp<R, FORCE>(F, r, vx, vy, vz, C);
+            collide_sp<R, FORCE, Cd::DEV>(F, r, vx, vy, vz, C);
             store_node<STORE>(F, fout, n, r, rref_out);
         }
         if constexpr (CHECK) {
@@ -157,7 +157,7 @@ __global__ void batch_init_kernel(const __grid_constant__ SpConsts<typename Code
     if constexpr (Cd::DEV) lbm_feq_dev_all<R>((R)0, (R)0, (R)0, (R)0, F);
     else lbm_feq_all<R>((R)1, (R)0, (R)0, (R)0, F);
     const R r = Cd::DEV ? (R)0 : (R)1;
-    collide_sp<R, FORCE>(F, r, (R)0, (R)0, (R)0, C);
+    collide_sp<R, FORCE, Cd::DEV>(F, r, (R)0, (R)0, (R)0, C);
     store_node<STORE>(F, fout, n, r, rref_out);
 }
 

@@ -118,10 +118,13 @@ __device__ __forceinline__ R vsum(const R* F) {
 
 // Class collision (SP:222-241): F, rho, v -> f (in place).  In deviation form
 // F holds f - w and r is rho - 1 (moment 0 of M (f - w)).
-template <typename R, bool FORCE>
+// FAST (deviation-form kernels): pair-form transforms and FMA relaxation; the
+// reference-arithmetic kernels keep the term-by-term order (FAST = false).
+template <typename R, bool FORCE, bool FAST = false>
 __device__ __forceinline__ void collide_sp(R* F, R r, R vx, R vy, R vz, const SpConsts<R>& C) {
     R m[19];
-    mrt_moments<R>(F, m);
+    if constexpr (FAST) mrt_moments_fast<R>(F, m);
+    else mrt_moments<R>(F, m);
     const R uu = lbm_usq(vx, vy, vz);
     R meq[19];
 #pragma unroll
@@ -135,7 +138,8 @@ __device__ __forceinline__ void collide_sp(R* F, R r, R vx, R vy, R vz, const Sp
         const int kd = lbm_skind(s);
         if (kd == 0) continue;
         const R S = kd == 1 ? C.sv : C.so;
-        m[s] = m[s] - S * (m[s] - meq[s]);
+        if constexpr (FAST) m[s] = lbm_fma<R>(S, meq[s] - m[s], m[s]);
+        else m[s] = m[s] - S * (m[s] - meq[s]);
     }
     if constexpr (FORCE) {
         const R fx = C.fext[0], fy = C.fext[1], fz = C.fext[2];
@@ -159,15 +163,18 @@ __device__ __forceinline__ void collide_sp(R* F, R r, R vx, R vy, R vz, const Sp
             G[l] = (R)lbm_w(l) * g;
         }
         R fg[19];
-        mrt_moments<R>(G, fg);
+        if constexpr (FAST) mrt_moments_fast<R>(G, fg);
+        else mrt_moments<R>(G, fg);
 #pragma unroll
         for (int s = 0; s < 19; ++s) {
             const int kd = lbm_skind(s);
             const R S = kd == 0 ? (R)0 : (kd == 1 ? C.sv : C.so);
-            m[s] = m[s] + ((R)1 - (R)0.5 * S) * fg[s];
+            if constexpr (FAST) m[s] = lbm_fma<R>((R)1 - (R)0.5 * S, fg[s], m[s]);
+            else m[s] = m[s] + ((R)1 - (R)0.5 * S) * fg[s];
         }
     }
-    mrt_back<R>(m, F);
+    if constexpr (FAST) mrt_back_fast<R>(m, F);
+    else mrt_back<R>(m, F);
 }
 
 // Face boundary conditions for one node on >= 1 non-periodic face

@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(256, STORE == LBM_STORE_F64 ? 1 : (FORCE ? 4 :
         v_out[2 * np + n] = vz;
     }
 
-    collide_sp<R, FORCE>(F, r, vx, vy, vz, C);
+    collide_sp<R, FORCE, Cd::DEV>(F, r, vx, vy, vz, C);
     store_node<STORE>(F, fout, n, r, rref_out);
 }
 
@@ -115,7 +115,7 @@ __global__ void sp_init_kernel(const __grid_constant__ SpConsts<typename Codec<S
     vprev[np + n] = vy;
     vprev[2 * np + n] = vz;
     const R r = Cd::DEV ? rd : (R)1 + rd;
-    collide_sp<R, FORCE>(F, r, vx, vy, vz, C);
+    collide_sp<R, FORCE, Cd::DEV>(F, r, vx, vy, vz, C);
     store_node<STORE>(F, fout, n, r, rref_out);
 }
 

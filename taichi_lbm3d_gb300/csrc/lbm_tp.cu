@@ -127,11 +127,12 @@ __device__ __forceinline__ void recolour_amounts(R rr, R rb, R vx, R vy, R vz, R
 }
 
 // Two-phase MRT collision (TP:302-344) of F in place.
-template <typename R, bool FORCE>
+template <typename R, bool FORCE, bool FAST>
 __device__ __forceinline__ void collide_tp(R* F, R r, R vx, R vy, R vz, R cc, R n0, R n1, R n2, R sv, R so,
                                            const TpConsts<R>& T) {
     R m[19];
-    mrt_moments<R>(F, m);
+    if constexpr (FAST) mrt_moments_fast<R>(F, m);
+    else mrt_moments<R>(F, m);
     R meq[19];
 #pragma unroll
     for (int s = 0; s < 19; ++s) meq[s] = (R)0;
@@ -152,7 +153,8 @@ __device__ __forceinline__ void collide_tp(R* F, R r, R vx, R vy, R vz, R cc, R 
         const int kd = lbm_skind(s);
         if (kd == 0) continue;
         const R S = kd == 1 ? sv : so;
-        m[s] = m[s] - S * (m[s] - meq[s]);
+        if constexpr (FAST) m[s] = lbm_fma<R>(S, meq[s] - m[s], m[s]);
+        else m[s] = m[s] - S * (m[s] - meq[s]);
     }
     if constexpr (FORCE) {
         const R fx = T.sp.fext[0], fy = T.sp.fext[1], fz = T.sp.fext[2];
@@ -172,15 +174,18 @@ __device__ __forceinline__ void collide_tp(R* F, R r, R vx, R vy, R vz, R cc, R 
             G[l] = (R)lbm_w(l) * (a + eu * ef);  // GuoF, TP:242-248
         }
         R fg[19];
-        mrt_moments<R>(G, fg);
+        if constexpr (FAST) mrt_moments_fast<R>(G, fg);
+        else mrt_moments<R>(G, fg);
 #pragma unroll
         for (int s = 0; s < 19; ++s) {
             const int kd = lbm_skind(s);
             const R S = kd == 0 ? (R)0 : (kd == 1 ? sv : so);
-            m[s] = m[s] + ((R)1 - (R)0.5 * S) * fg[s];
+            if constexpr (FAST) m[s] = lbm_fma<R>((R)1 - (R)0.5 * S, fg[s], m[s]);
+            else m[s] = m[s] + ((R)1 - (R)0.5 * S) * fg[s];
         }
     }
-    mrt_back<R>(m, F);
+    if constexpr (FAST) mrt_back_fast<R>(m, F);
+    else mrt_back<R>(m, F);
 }
 
 // Everything B does after the macros: colour gradient, collision, recolouring.
@@ -208,7 +213,7 @@ __device__ __forceinline__ void tp_collide_and_store(typename Codec<STORE>::R* F
     }
     R sv, so;
     s_local<R>(T, psi[n], sv, so);
-    collide_tp<R, FORCE>(F, r, vx, vy, vz, cc, n0, n1, n2, sv, so, T);
+    collide_tp<R, FORCE, Cd::DEV>(F, r, vx, vy, vz, cc, n0, n1, n2, sv, so, T);
     store_node<STORE>(F, fout, n, r, rref_out);
     R cs[9];
     recolour_amounts<R>(rr, rb, vx, vy, vz, Cx, Cy, Cz, cc, cs);
