@@ -35,7 +35,7 @@ sys.path.insert(0, ROOT)
 SHAPE = (256, 256, 256)
 PACK = dict(rmin=4.0, rmax=10.0, porosity=0.35, seed=2)
 RHO_IN, RHO_OUT, NIU = 1.0005, 1.0, 0.1
-BYTES_PER_NODE = {"f32": 152, "f16": 76, "bf16": 76, "f64": 304}
+BYTES_PER_NODE = {"f32": 152, "f32dev": 152, "f16": 76, "bf16": 76, "f64": 304}
 METRIC = "MLUPS"
 UNIT = "MLUPS (1e6 fluid-node updates per second)"
 PROFILE_MD = os.path.join(ROOT, "profiles", "sp_step_kernel_f32_porous256.md")
@@ -486,7 +486,7 @@ def main():
     if rank == 0:
         if not a.no_variants:
             var = {}
-            for sto in ("f16", "bf16"):
+            for sto in ("f32dev", "f16", "bf16"):
                 nfv, sv = run_variant(solid, sto, min(a.steps, 1000), warmup)
                 var[sto] = {"value": nfv * min(a.steps, 1000) / sv / 1e6, "unit": UNIT,
                             "gbs_algorithmic": BYTES_PER_NODE[sto] * nfv * min(a.steps, 1000) / sv / 1e9}
