@@ -375,6 +375,110 @@ def two_phase(steps=20000, every=500, shape=(131, 131, 131), storages=("f64", "f
     return out
 
 
+def grey_field(shape=SHAPE):
+    """Grey-scale workload: the 256^3 pack of the default bench with ns = 1 in
+    the spheres and a grey layer ns = 0.25 on pore cells within 1.5 cells of a
+    sphere (unresolved roughness), ns = 0 elsewhere."""
+    from taichi_lbm3d_gb300.geometry import distance_to_solid
+    solid = geometry() if shape == SHAPE else None
+    if solid is None:
+        from taichi_lbm3d_gb300.geometry import sphere_pack
+        solid = sphere_pack(shape, PACK["rmin"], PACK["rmax"], PACK["porosity"], PACK["seed"])
+    ns = np.where(solid > 0, 1.0, 0.0)
+    ns[(solid == 0) & (distance_to_solid(solid) <= 1.5)] = 0.25
+    return ns
+
+
+def grey(steps=1000, cpu_seconds=20.0, log=lambda m: print(m, file=sys.stderr, flush=True)):
+    """Grey-scale (partial bounce-back) step on the grey 256^3 field: body
+    force fx = 1e-6, periodic, niu 0.1 (script conventions).  MLUPS with CUDA
+    events on the library's stream, FP32 and FP16; the CPU oracle's grey sweeps
+    on a bounded sample of the same lattice."""
+    import torch
+    from taichi_lbm3d_gb300 import LB3D_Solver_Grey_Scale
+    ns = grey_field()
+    nf = int((ns < 1.0).sum())
+    out = {"workload": "grey-scale step, 256^3 pack (seed 2) with ns = 1 spheres and an ns = 0.25 layer "
+                       "within 1.5 cells of them, fx 1e-6, periodic, niu 0.1",
+           "n_fluid": nf, "n_grey": int(((ns > 0) & (ns < 1)).sum()), "steps": steps}
+    peak, kind = measured_peak()
+    for sto in ("f32", "f16"):
+        lb = LB3D_Solver_Grey_Scale(*SHAPE, storage=sto)
+        lb.fx = 1e-6
+        lb.ns.from_numpy(ns)
+        lb.solid.from_numpy(ns.astype(int))
+        lb.init_simulation()
+        lat = lb._lat
+        stream = torch.cuda.ExternalStream(lat.stream())
+        lat.step_async(20)
+        lat.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        lat.step_async(steps)
+        e1.record(stream)
+        e1.synchronize()
+        secs = e0.elapsed_time(e1) / 1e3
+        mlups = nf * steps / secs / 1e6
+        # algorithmic bytes per node: populations in + out, plus the node's ns
+        bpn = {"f32": 156, "f16": 80}[sto]
+        out["mlups_" + sto] = mlups
+        out["gbs_algorithmic_" + sto] = bpn * mlups / 1e3
+        out["roofline_frac_" + sto] = bpn * mlups / 1e3 / peak
+        st = lb.stats()
+        out["max_v_" + sto] = st.max_v
+        log("grey %s: %.0f MLUPS (%.0f GB/s algorithmic, %.1f%% of %s HBM copy)" % (
+            sto, mlups, bpn * mlups / 1e3, 100 * bpn * mlups / 1e3 / peak, kind))
+        lb.close()
+    from oracle.oracle import Oracle, make_params
+    p = make_params(SHAPE, niu=0.1, force=(1e-6, 0, 0), visc_convention=1, guo_convention=1, bc_form=1, grey=True)
+    o = Oracle(p, (ns.astype(int) != 0).astype(np.int8))
+    o.set_field("ns", ns)
+    o.step(1)
+    n, t = 0, 0.0
+    while t < cpu_seconds and n < 50:
+        t0 = time.perf_counter()
+        o.step(1)
+        t += time.perf_counter() - t0
+        n += 1
+    o.close()
+    out["cpu_baseline"] = {"value": nf * n / t / 1e6, "unit": UNIT, "cores": len(os.sched_getaffinity(0)),
+                           "kind": "port", "sample": "%d grey steps of the full 256^3 lattice (%.1f s)" % (n, t)}
+    out["peak_gbs"] = peak
+    out["peak_kind"] = kind
+    return out
+
+
+def voxelize_bench(log=lambda m: print(m, file=sys.stderr, flush=True)):
+    """STL voxeliser: NACA 0012 wing (chord 40, span 20, 80 stations) in the
+    reference tool's box (-10..50, -5..5, -15..15) at dx 0.5 (its setting) and
+    0.1; GPU wall time per call (upload, kernel, download) and the FP64 CPU
+    oracle on the dx 0.5 grid."""
+    from taichi_lbm3d_gb300 import voxelize as vx
+    from oracle import oracle
+    tris = vx.naca4_wing("0012")
+    out = {"triangles": int(len(tris))}
+    vx.voxelize(tris, vx.REF_LO, vx.REF_HI, 1.0)           # context + module load
+    for dx in (0.5, 0.1):
+        dims = vx.grid_dims(vx.REF_LO, vx.REF_HI, dx)
+        best = float("inf")
+        for _ in range(3):
+            t0 = time.perf_counter()
+            solid = vx.voxelize(tris, vx.REF_LO, vx.REF_HI, dx)
+            best = min(best, time.perf_counter() - t0)
+        npts = int(np.prod(dims))
+        out["dx_%g" % dx] = {"dims": list(dims), "seconds": best, "solid_fraction": float(solid.mean()),
+                             "gpairs_per_s": npts * len(tris) / best / 1e9}
+        log("voxelise dx %g: %s points in %.3f s" % (dx, dims, best))
+    dims = vx.grid_dims(vx.REF_LO, vx.REF_HI, 0.5)
+    t0 = time.perf_counter()
+    o_solid, _ = oracle.voxelize(tris, vx.REF_LO, 0.5, dims)
+    secs = time.perf_counter() - t0
+    g_solid = vx.voxelize(tris, vx.REF_LO, vx.REF_HI, 0.5)
+    out["cpu_oracle_dx_0.5"] = {"seconds": secs, "cores": len(os.sched_getaffinity(0)),
+                                "flags_equal_gpu": bool(np.array_equal(o_solid, g_solid))}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -389,7 +493,15 @@ def main():
                     help="config 4: batched persistent launch vs serial plain kernel, k error vs FP64")
     ap.add_argument("--n-sub", type=int, default=256)
     ap.add_argument("--two-phase", action="store_true", help="config 3: two-phase drainage vs FP64")
+    ap.add_argument("--grey", action="store_true", help="grey-scale (partial bounce-back) step on a 256^3 grey field")
+    ap.add_argument("--voxelize", action="store_true", help="STL voxeliser on a NACA wing in the reference box")
     a = ap.parse_args()
+    if a.voxelize:
+        print(json.dumps({"voxelize": voxelize_bench()}))
+        return 0
+    if a.grey:
+        print(json.dumps({"grey": grey()}))
+        return 0
     if a.two_phase:
         print(json.dumps({"two_phase": two_phase()}))
         return 0

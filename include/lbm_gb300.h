@@ -79,7 +79,7 @@ typedef struct LbmParams {
     int32_t psi_bc[6];       /* TP:35-40: 0 periodic, 1 constant psi */
     double psi_val[6];
     int32_t device;          /* CUDA device ordinal */
-    int32_t block_size;      /* threads per CTA of the step kernel, 0 = default */
+    int32_t block_size;      /* threads per CTA of the step kernel, 0 = default (128 single-phase, 256 two-phase) */
 } LbmParams;
 
 typedef struct LbmInfo {
@@ -118,6 +118,15 @@ int lbm_set_geometry(LbmHandle* h, const int8_t* solid);
 
 /* Two-phase initial phase field psi[cell] (TP:195-203, psi.from_numpy). */
 int lbm_set_psi(LbmHandle* h, const float* psi);
+
+/* Grey-scale lattice: partial bounce-back fraction ns[cell] of every cell
+ * (ns.from_numpy, Grey_Scale/lbm_solver_3d_Macro_Sukop.py:320-324; the caller
+ * passes the solid mask ns.astype(int) != 0 to lbm_set_geometry first).  The
+ * step then runs the script's streaming0/streaming1 rule (:234-252) in place
+ * of halfway bounce-back.  Fixed faces on x only (LBM_EINVAL otherwise, as
+ * the script's Boundary_condition treats x only, :263-293); call lbm_init
+ * afterwards.  A new lbm_set_geometry clears it. */
+int lbm_set_grey(LbmHandle* h, const double* ns);
 
 /* Initial state: rho = 1, v = 0, f = feq (init, SP:160-170 / TP:174-187) when
  * rho and v are NULL; otherwise f = feq(rho, v) from the given dense fields

@@ -9,8 +9,9 @@
  * Reference files restated (paths inside the taichi_LBM3D checkout):
  *   Single_phase/LBM_3D_SinglePhase_Solver.py   lines 9-481  (single phase, class)
  *   2phase/lbm_solver_3d_2phase_sparse.py        lines 99-606 (two phase, script)
+ *   Grey_Scale/lbm_solver_3d_Macro_Sukop.py      lines 112-336 (grey scale, script)
  *
- * Parity pinning: tests/golden/make_golden.py runs those two reference files
+ * Parity pinning: tests/golden/make_golden.py runs those reference files
  * unmodified on small lattices (through a numpy stand-in for Taichi) and
  * stores their outputs; tests/test_oracle_golden.py checks this oracle against
  * every fixture.
@@ -43,6 +44,9 @@ typedef struct OracleParams {
      *        of colission's += would; bit 1: sv taken as the Python double wl/wg
      *        (then sother in FP64) where Compute_S_local assigns the constant. */
     int32_t ref_emulation;
+    /* Grey-scale script (partial bounce-back, Grey_Scale/lbm_solver_3d_Macro_Sukop.py):
+     * per-cell ns set through lbm_oracle_set(what = 8); x faces only. */
+    int32_t grey;
 } OracleParams;
 
 /* e, w, LR: LBM_3D_SinglePhase_Solver.py:183-197, :85 */
@@ -154,7 +158,7 @@ int lbm_oracle_stream_only(OracleHandle *h) {
                               : oracle_stream_only_f32((oracle_sp_f32 *)h->impl);
 }
 
-/* what: 0 rho, 1 v, 2 f, 3 F, 4 psi, 5 rho_r, 6 rho_b, 7 inv_M (19x19) */
+/* what: 0 rho, 1 v, 2 f, 3 F, 4 psi, 5 rho_r, 6 rho_b, 7 inv_M (19x19), 8 ns (grey) */
 int lbm_oracle_get(OracleHandle *h, int what, double *out) {
     if (!h || !out) return -1;
     return h->precision == 64 ? oracle_get_f64((oracle_sp_f64 *)h->impl, what, out)

@@ -27,6 +27,8 @@ typedef struct ST(oracle_sp_) {
     REAL *psi, *rho_r, *rho_b, *Gr, *Gb;  /* Gr/Gb: colour slots [cell*19+s] */
     REAL wl, wg, lg0, l1, l2, g1, g2, psi_solid, capa;
     double wl_d, wg_d;
+    /* grey scale */
+    REAL *ns, *f2;                   /* ns[cell], f2[cell*19+s] */
 } ST(oracle_sp_);
 
 static inline int64_t FN(cid_)(const OracleParams *p, int i, int j, int k) {
@@ -125,6 +127,12 @@ ST(oracle_sp_) *FN(oracle_create_)(const OracleParams *p, const int8_t *solid, c
         o->v[c * 3 + 0] = o->v[c * 3 + 1] = o->v[c * 3 + 2] = 0;
         for (int s = 0; s < 19; ++s) o->f[c * 19 + s] = o->F[c * 19 + s] = FN(feq_)(s, (REAL)1.0, zero);
     }
+    if (p->grey) {
+        /* ns = 0 until set; f2 as the script allocates it (:32) */
+        o->ns = (REAL *)calloc((size_t)n, sizeof(REAL));
+        o->f2 = (REAL *)calloc((size_t)n * 19, sizeof(REAL));
+        if (!o->ns || !o->f2) return NULL;
+    }
     if (p->two_phase) {
         o->psi = (REAL *)malloc(sizeof(REAL) * n);
         o->rho_r = (REAL *)malloc(sizeof(REAL) * n);
@@ -149,6 +157,7 @@ void FN(oracle_destroy_)(ST(oracle_sp_) *o) {
     if (!o) return;
     free(o->solid); free(o->f); free(o->F); free(o->rho); free(o->v);
     free(o->psi); free(o->rho_r); free(o->rho_b); free(o->Gr); free(o->Gb);
+    free(o->ns); free(o->f2);
     free(o);
 }
 
@@ -262,6 +271,45 @@ static void FN(bc_face_)(ST(oracle_sp_) *o, int face) {
                     Fc[s] = (FN(feq_)(LR[s], (REAL)1.0, ubc) - Fc[LR[s]]) + FN(feq_)(s, (REAL)1.0, ubc);
             }
         }
+}
+
+/* Grey scale, streaming0: Grey_Scale/lbm_solver_3d_Macro_Sukop.py:234-240.
+ * Partial bounce-back mixed with the opposite population of the neighbour the
+ * population moves to: f2[c,s] = f[c,s] + ns[c] (f[c+e_s, LR s] - f[c,s]).
+ * f at solid cells is never written after init (feq(s, 1, 0)). */
+static void FN(grey_stream0_)(ST(oracle_sp_) *o) {
+    const OracleParams *p = &o->p;
+#pragma omp parallel for schedule(static) collapse(2)
+    for (int k = 0; k < p->nz; ++k)
+        for (int j = 0; j < p->ny; ++j)
+            for (int i = 0; i < p->nx; ++i) {
+                int64_t c = FN(cid_)(p, i, j, k);
+                if (o->solid[c]) continue;
+                for (int s = 0; s < 19; ++s) {
+                    int64_t ip = FN(wrap_)(p, i + E[s][0], j + E[s][1], k + E[s][2]);
+                    const REAL a = o->f[c * 19 + s];
+                    o->f2[c * 19 + s] = a + o->ns[c] * (o->f[ip * 19 + LR[s]] - a);
+                }
+            }
+}
+
+/* Grey scale, streaming1: Grey_Scale/lbm_solver_3d_Macro_Sukop.py:243-252.
+ * Plain push of f2 from every fluid cell, also into solid cells; F of a fluid
+ * cell whose upstream cell is solid keeps its previous value. */
+static void FN(grey_stream1_)(ST(oracle_sp_) *o) {
+    const OracleParams *p = &o->p;
+    /* each (cell, s) slot has exactly one source cell, so the sweep is order-free */
+#pragma omp parallel for schedule(static) collapse(2)
+    for (int k = 0; k < p->nz; ++k)
+        for (int j = 0; j < p->ny; ++j)
+            for (int i = 0; i < p->nx; ++i) {
+                int64_t c = FN(cid_)(p, i, j, k);
+                if (o->solid[c]) continue;
+                for (int s = 0; s < 19; ++s) {
+                    int64_t ip = FN(wrap_)(p, i + E[s][0], j + E[s][1], k + E[s][2]);
+                    o->F[ip * 19 + s] = o->f2[c * 19 + s];
+                }
+            }
 }
 
 /* streaming3: LBM_3D_SinglePhase_Solver.py:372-392 */
@@ -489,7 +537,17 @@ static void FN(bc_psi_)(ST(oracle_sp_) *o) {
  * 2phase/lbm_solver_3d_2phase_sparse.py:626-632 (two phase). */
 int FN(oracle_step_)(ST(oracle_sp_) *o, int nsteps) {
     for (int it = 0; it < nsteps; ++it) {
-        if (o->p.two_phase) {
+        if (o->p.grey) {
+            /* Grey_Scale/lbm_solver_3d_Macro_Sukop.py:330-336; its
+             * Boundary_condition treats the x faces only (:263-293) and
+             * streaming3 (:296-312) is the single-phase macroscopic update */
+            FN(collide_sp_)(o);
+            FN(grey_stream0_)(o);
+            FN(grey_stream1_)(o);
+            FN(bc_face_)(o, 0);
+            FN(bc_face_)(o, 1);
+            FN(macros_sp_)(o);
+        } else if (o->p.two_phase) {
             FN(collide_tp_)(o);
             FN(stream_)(o);
             for (int face = 0; face < 6; ++face) FN(bc_face_)(o, face);
@@ -524,6 +582,7 @@ int FN(oracle_get_)(ST(oracle_sp_) *o, int what, double *out) {
     case 5: if (!o->rho_r) return -1; for (int64_t c = 0; c < n; ++c) out[c] = (double)o->rho_r[c]; break;
     case 6: if (!o->rho_b) return -1; for (int64_t c = 0; c < n; ++c) out[c] = (double)o->rho_b[c]; break;
     case 7: for (int r = 0; r < 19; ++r) for (int c = 0; c < 19; ++c) out[r * 19 + c] = (double)o->Minv[r][c]; break;
+    case 8: if (!o->ns) return -1; for (int64_t c = 0; c < n; ++c) out[c] = (double)o->ns[c]; break;
     default: return -1;
     }
     return 0;
@@ -534,6 +593,7 @@ int FN(oracle_set_)(ST(oracle_sp_) *o, int what, const double *in) {
     switch (what) {
     case 2: for (int64_t c = 0; c < n * 19; ++c) o->f[c] = (REAL)in[c]; break;
     case 3: for (int64_t c = 0; c < n * 19; ++c) o->F[c] = (REAL)in[c]; break;
+    case 8: if (!o->ns) return -1; for (int64_t c = 0; c < n; ++c) o->ns[c] = (REAL)in[c]; break;
     default: return -1;
     }
     return 0;

@@ -32,18 +32,19 @@ class OracleParams(ctypes.Structure):
         ("psi_bc", ctypes.c_int32 * 6),
         ("psi_val", ctypes.c_double * 6),
         ("ref_emulation", ctypes.c_int32),
+        ("grey", ctypes.c_int32),
     ]
 
 
 def build(force=False):
     """Compile the oracle with gcc (OpenMP, no FP contraction)."""
-    src = os.path.join(HERE, "lbm_oracle.c")
+    srcs = [os.path.join(HERE, f) for f in ("lbm_oracle.c", "vox_oracle.c")]
     body = os.path.join(HERE, "lbm_oracle_body.h")
     if (not force and os.path.exists(LIB_PATH)
-            and os.path.getmtime(LIB_PATH) >= max(os.path.getmtime(src), os.path.getmtime(body))):
+            and os.path.getmtime(LIB_PATH) >= max(os.path.getmtime(f) for f in srcs + [body])):
         return LIB_PATH
     cmd = ["gcc", "-O3", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
-           "-o", LIB_PATH, src, "-lm"]
+           "-o", LIB_PATH] + srcs + ["-lm"]
     subprocess.check_call(cmd, cwd=HERE)
     return LIB_PATH
 
@@ -64,6 +65,11 @@ def lib():
         L.lbm_oracle_get.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
         L.lbm_oracle_set.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
         assert L.lbm_oracle_sizeof_params() == ctypes.sizeof(OracleParams)
+        L.lbm_oracle_voxelize.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_float,
+                                          ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_float,
+                                          ctypes.c_void_p, ctypes.c_void_p]
+        L.lbm_oracle_mesh_distance.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_float,
+                                               ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p]
         _lib = L
     return _lib
 
@@ -71,7 +77,7 @@ def lib():
 def make_params(shape, niu=0.16667, force=(0.0, 0.0, 0.0), bc=(0,) * 6, rho_bc=(1.0,) * 6,
                 vel_bc=((0.0, 0.0, 0.0),) * 6, visc_convention=0, guo_convention=0, bc_form=0,
                 two_phase=False, niu_l=0.1, niu_g=0.1, psi_solid=0.7, cap_a=0.005,
-                psi_bc=(0,) * 6, psi_val=(1.0,) * 6, ref_emulation=0):
+                psi_bc=(0,) * 6, psi_val=(1.0,) * 6, ref_emulation=0, grey=False):
     p = OracleParams()
     p.nx, p.ny, p.nz = shape
     for f in range(6):
@@ -90,6 +96,7 @@ def make_params(shape, niu=0.16667, force=(0.0, 0.0, 0.0), bc=(0,) * 6, rho_bc=(
     p.two_phase = 1 if two_phase else 0
     p.niu_l, p.niu_g, p.psi_solid, p.cap_a = niu_l, niu_g, psi_solid, cap_a
     p.ref_emulation = ref_emulation
+    p.grey = 1 if grey else 0
     return p
 
 
@@ -133,7 +140,7 @@ class Oracle:
     def field(self, name):
         """Return a field as an (nx,ny,nz[,c]) array (Fortran cell order undone)."""
         what, comps = {"rho": (0, 1), "v": (1, 3), "f": (2, 19), "F": (3, 19), "psi": (4, 1),
-                       "rho_r": (5, 1), "rho_b": (6, 1)}[name]
+                       "rho_r": (5, 1), "rho_b": (6, 1), "ns": (8, 1)}[name]
         a = self._get(what, comps)
         if comps == 1:
             return a.reshape(self.shape, order="F")
@@ -143,8 +150,30 @@ class Oracle:
         return self._get(7, 1).reshape(19, 19)
 
     def set_field(self, name, arr):
-        what, comps = {"f": (2, 19), "F": (3, 19)}[name]
+        what, comps = {"f": (2, 19), "F": (3, 19), "ns": (8, 1)}[name]
         a = np.asarray(arr, dtype=np.float64).reshape(self.shape + (comps,))
         flat = np.ascontiguousarray(a.reshape((self.ncell, comps), order="F"))
         if lib().lbm_oracle_set(self.h, what, flat.ctypes.data) != 0:
             raise RuntimeError("oracle set failed")
+
+
+def voxelize(tris, origin, dx, dims, surf_eps=-1.0):
+    """FP64 oracle of the voxeliser: (solid int8 (nx,ny,nz), winding (nx,ny,nz))."""
+    t = np.ascontiguousarray(np.asarray(tris, np.float32).reshape(-1, 9))
+    o = np.ascontiguousarray(np.asarray(origin, np.float32))
+    nx, ny, nz = (int(x) for x in dims)
+    solid = np.empty(nx * ny * nz, np.int8)
+    w = np.empty(nx * ny * nz, np.float64)
+    if lib().lbm_oracle_voxelize(t.ctypes.data, t.shape[0], o.ctypes.data, float(dx), nx, ny, nz, float(surf_eps),
+                                 solid.ctypes.data, w.ctypes.data) != 0:
+        raise RuntimeError("oracle voxelize failed")
+    return solid.reshape((nx, ny, nz), order="F"), w.reshape((nx, ny, nz), order="F")
+
+
+def mesh_distance(tris, origin, dx, dims):
+    t = np.ascontiguousarray(np.asarray(tris, np.float32).reshape(-1, 9))
+    o = np.ascontiguousarray(np.asarray(origin, np.float32))
+    nx, ny, nz = (int(x) for x in dims)
+    d = np.empty(nx * ny * nz, np.float64)
+    lib().lbm_oracle_mesh_distance(t.ctypes.data, t.shape[0], o.ctypes.data, float(dx), nx, ny, nz, d.ctypes.data)
+    return d.reshape((nx, ny, nz), order="F")

@@ -12,5 +12,6 @@ through ctypes); there is no CPU fallback.
 """
 from .solver import LB3D_Solver_Single_Phase  # noqa: F401
 from .two_phase import LB3D_Solver_Two_Phase  # noqa: F401
+from .grey import LB3D_Solver_Grey_Scale  # noqa: F401
 
-__all__ = ["LB3D_Solver_Single_Phase", "LB3D_Solver_Two_Phase"]
+__all__ = ["LB3D_Solver_Single_Phase", "LB3D_Solver_Two_Phase", "LB3D_Solver_Grey_Scale"]

@@ -63,6 +63,7 @@ SIGNATURES = {
     "lbm_destroy": [_P],
     "lbm_set_geometry": [_P, _P],
     "lbm_set_psi": [_P, _P],
+    "lbm_set_grey": [_P, _P],
     "lbm_init": [_P, _P, _P],
     "lbm_step": [_P, ctypes.c_int32],
     "lbm_step_async": [_P, ctypes.c_int32],
@@ -158,6 +159,13 @@ class Lattice:
     def set_psi(self, psi):
         a = np.ascontiguousarray(np.asarray(psi, dtype=np.float32).ravel(order="F"))
         self._c(load().lbm_set_psi(self.h, ptr(a)))
+
+    def set_grey(self, ns):
+        """Partial bounce-back fraction per cell (call after set_geometry)."""
+        a = np.ascontiguousarray(np.asarray(ns, dtype=np.float64).ravel(order="F"))
+        if a.size != self.ncell:
+            raise ValueError("ns has %d cells, lattice has %d" % (a.size, self.ncell))
+        self._c(load().lbm_set_grey(self.h, ptr(a)))
 
     def init(self, rho=None, v=None):
         if rho is None:

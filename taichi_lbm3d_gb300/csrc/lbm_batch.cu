@@ -3,8 +3,12 @@
 //
 // Layout: the compacted fluid nodes of all subvolumes are concatenated (each
 // subvolume starts on a multiple of 32 so no population chunk straddles two);
-// each subvolume has its own dense node map (global node indices).  Work is cut
-// into tiles (subvolume, node range); the grid is sized to the resident CTAs of
+// each subvolume has its own dense node map holding node indices local to the
+// subvolume.  A CTA offsets the population, coordinate and density-reference
+// arrays to its subvolume's first node once (64-bit), and the 32-bit offset
+// arithmetic of the gather stays local, so the batch as a whole may exceed
+// 2^31 population elements.  Work is cut into tiles (subvolume, local node
+// range); the grid is sized to the resident CTAs of
 // the GPU and CTAs claim tiles from an atomic counter, so uneven subvolumes
 // share the GPU without tail effects.  Converged subvolumes are removed by
 // rewriting the tile list in device memory between graph launches; the graph
@@ -24,14 +28,24 @@
 #include "lbm_kernels.cuh"
 
 struct BatchSub {
-    int32_t nx, ny, nz, pad;
-    int64_t map_off;
-    int32_t node_begin, n_fluid;
+    int32_t nx, ny, nz, n_fluid;
+    int64_t map_off;        // first cell of this subvolume's dense map
+    int64_t node_begin;     // first node (a multiple of 32) in the concatenated arrays
 };
 
 struct BatchTile {
-    int32_t sub, begin, end, pad;
+    int32_t sub, begin, end, pad;   // local node range [begin, end)
 };
+
+// Per-subvolume views of the concatenated arrays (node indices become local).
+template <typename T>
+__device__ __forceinline__ T* sub_pop(T* f, int64_t node_begin) {
+    return f + lbm_eoff(node_begin);
+}
+template <typename T>
+__device__ __forceinline__ T* sub_node(T* a, int64_t node_begin) {
+    return a ? a + node_begin : a;
+}
 
 struct LbmBatch {
     LbmHandle h;                        // shared params, stream, populations, coords, map
@@ -79,12 +93,17 @@ __global__ void __launch_bounds__(256, STORE == LBM_STORE_F64 ? 1 : 4) batch_ste
         const BatchTile tl = tiles[t];
         const BatchSub sd = subs[tl.sub];
         const int32_t* smap = map + sd.map_off;
+        const typename Cd::T* sfin = sub_pop(fin, sd.node_begin);
+        typename Cd::T* sfout = sub_pop(fout, sd.node_begin);
+        const uint32_t* scoord = coord + sd.node_begin;
+        const float* srin = sub_node(rref_in, sd.node_begin);
+        float* srout = sub_node(rref_out, sd.node_begin);
         double acc = 0.0;
         for (int n = tl.begin + threadIdx.x; n < tl.end; n += blockDim.x) {
-            const uint32_t pc = __ldg(coord + n);
+            const uint32_t pc = __ldg(scoord + n);
             const int i = lbm_pi(pc), j = lbm_pj(pc), k = lbm_pk(pc);
             R F[19];
-            gather_node<STORE>(F, fin, smap, n, sd.nx, sd.ny, sd.nz, i, j, k, rref_in);
+            gather_node<STORE>(F, sfin, smap, n, sd.nx, sd.ny, sd.nz, i, j, k, srin);
             R r = F[0];
 #pragma unroll
             for (int s = 1; s < 19; ++s) r = r + F[s];
@@ -97,7 +116,7 @@ __global__ void __launch_bounds__(256, STORE == LBM_STORE_F64 ? 1 : 4) batch_ste
             }
             if constexpr (CHECK) acc += (double)vx;
             collide_sp<R, FORCE, Cd::DEV>(F, r, vx, vy, vz, C);
-            store_node<STORE>(F, fout, n, r, rref_out);
+            store_node<STORE>(F, sfout, n, r, srout);
         }
         if constexpr (CHECK) {
             for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
@@ -124,10 +143,10 @@ __global__ void batch_macros_kernel(const __grid_constant__ SpConsts<typename Co
     using R = typename Cd::R;
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= sd.n_fluid) return;
-    const int n = sd.node_begin + a;
-    const uint32_t pc = __ldg(coord + n);
+    const uint32_t pc = __ldg(coord + sd.node_begin + a);
     R F[19];
-    gather_node<STORE>(F, fin, map + sd.map_off, n, sd.nx, sd.ny, sd.nz, lbm_pi(pc), lbm_pj(pc), lbm_pk(pc), rref_in);
+    gather_node<STORE>(F, sub_pop(fin, sd.node_begin), map + sd.map_off, a, sd.nx, sd.ny, sd.nz, lbm_pi(pc), lbm_pj(pc),
+                       lbm_pk(pc), sub_node(rref_in, sd.node_begin));
     R r = F[0];
 #pragma unroll
     for (int s = 1; s < 19; ++s) r = r + F[s];
@@ -150,15 +169,16 @@ __global__ void batch_init_kernel(const __grid_constant__ SpConsts<typename Code
                                   int n_sub, float* __restrict__ rref_out) {
     using Cd = Codec<STORE>;
     using R = typename Cd::R;
+    if (blockIdx.y >= (unsigned)n_sub) return;
     const BatchSub sd = subs[blockIdx.y];
-    const int n = sd.node_begin + blockIdx.x * blockDim.x + threadIdx.x;
-    if (blockIdx.y >= (unsigned)n_sub || n >= sd.node_begin + sd.n_fluid) return;
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= sd.n_fluid) return;
     R F[19];
     if constexpr (Cd::DEV) lbm_feq_dev_all<R>((R)0, (R)0, (R)0, (R)0, F);
     else lbm_feq_all<R>((R)1, (R)0, (R)0, (R)0, F);
     const R r = Cd::DEV ? (R)0 : (R)1;
     collide_sp<R, FORCE, Cd::DEV>(F, r, (R)0, (R)0, (R)0, C);
-    store_node<STORE>(F, fout, n, r, rref_out);
+    store_node<STORE>(F, sub_pop(fout, sd.node_begin), n, r, sub_node(rref_out, sd.node_begin));
 }
 
 int batch_err(LbmBatch* b, int code, const std::string& m) { return lbm_set_err(&b->h, code, m); }
@@ -253,7 +273,7 @@ int rebuild_tiles(LbmBatch* b) {
         const BatchSub& s = b->subs[q];
         const int len = std::max(32, b->tile_len[q]);
         for (int a = 0; a < s.n_fluid; a += len)
-            b->tiles.push_back({(int32_t)q, s.node_begin + a, s.node_begin + std::min(s.n_fluid, a + len), 0});
+            b->tiles.push_back({(int32_t)q, a, std::min(s.n_fluid, a + len), 0});
     }
     LbmHandle* h = &b->h;
     if ((int64_t)b->tiles.size() > b->max_tiles) return batch_err(b, LBM_EINVAL, "tile list exceeds its allocation");
@@ -320,29 +340,33 @@ int lbm_batch_create(const LbmParams* params, int32_t n_sub, const int32_t* dims
     for (int q = 0; q < n_sub; ++q) {
         const int nx = dims[3 * q], ny = dims[3 * q + 1], nz = dims[3 * q + 2];
         if (nx < 1 || ny < 1 || nz < 1 || nx > 2047 || ny > 2047 || nz > 1023) {
-            delete b;
+            lbm_batch_destroy(b);
             return lbm_set_err(nullptr, LBM_EINVAL, "lbm_batch_create: bad subvolume size");
         }
         const int64_t nc = (int64_t)nx * ny * nz;
-        BatchSub s{nx, ny, nz, 0, (int64_t)map.size(), (int32_t)nodes, 0};
+        BatchSub s{nx, ny, nz, 0, (int64_t)map.size(), nodes};
         const int8_t* sol = solids + cells;
-        int32_t nf = 0;
+        int64_t nf = 0;
         map.resize(map.size() + nc);
         for (int64_t c = 0; c < nc; ++c) {
             if (sol[c] > 0) { map[s.map_off + c] = -1; continue; }
-            map[s.map_off + c] = (int32_t)(nodes + nf);
+            map[s.map_off + c] = (int32_t)nf;   // checked against the local limit below
             const int i = (int)(c % nx), j = (int)((c / nx) % ny), k = (int)(c / ((int64_t)nx * ny));
             coord.push_back(lbm_pack(i, j, k));
             ++nf;
         }
-        s.n_fluid = nf;
+        if (nf >= ((int64_t)1 << 31) / 19) {
+            lbm_batch_destroy(b);
+            return lbm_set_err(nullptr, LBM_EINVAL, "lbm_batch_create: subvolume has too many fluid nodes");
+        }
+        s.n_fluid = (int32_t)nf;
         const int64_t padded = (nf + 31) / 32 * 32;
         coord.resize(coord.size() + (padded - nf), 0);
         nodes += padded;
         cells += nc;
         b->subs.push_back(s);
     }
-    if (nodes >= ((int64_t)1 << 31) / 19) { delete b; return lbm_set_err(nullptr, LBM_EINVAL, "lbm_batch_create: too many nodes"); }
+    if (nodes >= ((int64_t)1 << 31) - 64) { lbm_batch_destroy(b); return lbm_set_err(nullptr, LBM_EINVAL, "lbm_batch_create: too many nodes"); }
     h->n_fluid = (int32_t)nodes;
     h->np = (nodes + 63) / 64 * 64;
     coord.resize(h->np, 0);
@@ -576,7 +600,7 @@ int lbm_batch_get_macros(LbmBatch* b, int32_t sub, float* rho, float* v) {
             rho[c] = 1.0f;
             v[3 * c] = v[3 * c + 1] = v[3 * c + 2] = 0.0f;
         } else {
-            const int64_t a = nd - sd.node_begin;
+            const int64_t a = nd;
             rho[c] = tmp[4 * a];
             for (int d = 0; d < 3; ++d) v[3 * c + d] = tmp[4 * a + 1 + d];
         }

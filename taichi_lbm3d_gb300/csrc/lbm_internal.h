@@ -60,6 +60,10 @@ struct LbmHandle {
     void* d_rb[2] = {nullptr, nullptr};    // rho_b
     void* d_cs = nullptr;                  // recolouring amounts of the 9 pairs [9][np]
     int ccur = 0;
+    // grey scale (partial bounce-back)
+    bool grey = false;
+    void* d_ns = nullptr;                  // [np] grey value per node (compute type)
+    void* d_gstale = nullptr;              // [2][ny*nz][19] post-face F of fixed-velocity x faces
     // reductions
     double* d_red = nullptr;               // per-block partials
     int red_blocks = 0;
@@ -77,6 +81,9 @@ int sp_launch_steps(LbmHandle* h, int32_t n, bool macros_last);
 int sp_launch_debug_stream(LbmHandle* h, const float* d_in, float* d_out);
 template <typename R>
 SpConsts<R> sp_make_consts(const LbmHandle* h);
+
+// grey scale (lbm_grey.cu)
+int grey_launch_steps(LbmHandle* h, int32_t n, bool macros_last);
 
 // two phase (lbm_tp.cu)
 int tp_launch_init(LbmHandle* h);

@@ -29,6 +29,20 @@ __device__ __forceinline__ Rows make_rows(int nx, int ny, int i, int j, int k, i
     return R;
 }
 
+// Node index of the pull source x - e_S of a node (or -1 when that cell is solid).
+template <int S, bool XWRAP>
+__device__ __forceinline__ int pull_source(const int32_t* __restrict__ map, const Rows& rows, int i, int xm, int xp) {
+    constexpr int ex = lbm_ex(S), ey = lbm_ey(S), ez = lbm_ez(S);
+    // source is x - e_S: row index 0 holds y-1 (used when ey = +1)
+    const int row = rows.r[1 - ey][1 - ez];
+    if constexpr (XWRAP) {
+        const int x = ex > 0 ? xm : (ex < 0 ? xp : i);
+        return __ldg(map + (row - i + x));
+    } else {
+        return __ldg(map + row - ex);
+    }
+}
+
 template <int STORE, bool XWRAP>
 struct Gather {
     using Cd = Codec<STORE>;
@@ -38,16 +52,7 @@ struct Gather {
     static __device__ __forceinline__ void one(R* F, const T* __restrict__ fin, const T* __restrict__ own,
                                                const int32_t* __restrict__ map, const Rows& rows, int i, int xm,
                                                int xp, const float* __restrict__ rref, int n) {
-        constexpr int ex = lbm_ex(S), ey = lbm_ey(S), ez = lbm_ez(S);
-        // source is x - e_S: row index 0 holds y-1 (used when ey = +1)
-        const int row = rows.r[1 - ey][1 - ez];
-        int src;
-        if constexpr (XWRAP) {
-            const int x = ex > 0 ? xm : (ex < 0 ? xp : i);
-            src = __ldg(map + (row - i + x));
-        } else {
-            src = __ldg(map + row - ex);
-        }
+        const int src = pull_source<S, XWRAP>(map, rows, i, xm, xp);
         if (src >= 0) F[S] = Cd::template dec<S>(fin[lbm_eoff32(src) + 32 * S]);
         else F[S] = Cd::template dec<S>(own[32 * lbm_lr(S)]);
         if constexpr (Cd::RHOREF) F[S] = lbm_fma<R>((R)lbm_w(S), (R)rref[src >= 0 ? src : n], F[S]);

@@ -211,6 +211,7 @@ template SpConsts<float> sp_make_consts<float>(const LbmHandle*);
 template SpConsts<double> sp_make_consts<double>(const LbmHandle*);
 
 int sp_launch_steps(LbmHandle* h, int32_t n, bool macros_last) {
+    if (h->grey) return grey_launch_steps(h, n, macros_last);
     switch (h->p.storage) {
     case LBM_STORE_F32: return run_steps<LBM_STORE_F32>(h, n, macros_last);
     case LBM_STORE_F16_DEV: return run_steps<LBM_STORE_F16_DEV>(h, n, macros_last);

@@ -25,13 +25,14 @@ def read_ascii_geometry(filename, shape):
     return solid.reshape(shape, order="F")
 
 
-def read_ascii_field(filename, shape):
-    """Float32 field of the lattice shape from an ASCII file, x fastest."""
+def read_ascii_field(filename, shape, dtype=np.float32):
+    """Field of the lattice shape from an ASCII file, x fastest (float32 unless
+    ``dtype`` says otherwise; np.loadtxt's float64 for the grey-scale ns)."""
     vals = _read_numbers(filename)
     n = int(np.prod(shape))
     if vals.size != n:
         raise ValueError("%s holds %d values, lattice %s needs %d" % (filename, vals.size, shape, n))
-    return vals.astype(np.float32).reshape(shape, order="F")
+    return vals.astype(dtype).reshape(shape, order="F")
 
 
 def write_ascii_geometry(filename, solid, fmt="%d"):

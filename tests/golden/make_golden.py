@@ -6,9 +6,10 @@ Run in a container that has the reference checkout (read-only) at
     python tests/golden/make_golden.py [--ref PATH] [--only NAME ...]
 
 Taichi is not installable offline, so ``taichi_numpy_shim`` stands in for it:
-the reference's kernel bodies (``Single_phase/LBM_3D_SinglePhase_Solver.py``
-and ``2phase/lbm_solver_3d_2phase_sparse.py``) execute unmodified as Python
-over FP32 numpy fields.  The two-phase script is a module-level program; its
+the reference's kernel bodies (``Single_phase/LBM_3D_SinglePhase_Solver.py``,
+``2phase/lbm_solver_3d_2phase_sparse.py`` and
+``Grey_Scale/lbm_solver_3d_Macro_Sukop.py``) execute unmodified as Python over
+FP32 numpy fields.  The two scripts are module-level programs; their
 parameter lines (lattice size, BC codes, physical constants) are edited the way
 its README tells a user to edit them, and the file is cut before its main loop
 (``time_init = time.time()``); kernel bodies are not touched.
@@ -291,6 +292,104 @@ def gen_two_phase(ref, only):
         case_tp(ref, "tp_velbc", p, solid, psi0.astype(np.float32), [1, 6])
 
 
+# ------------------------------------------------------- grey-scale script
+GREY_FILE = os.path.join("Grey_Scale", "lbm_solver_3d_Macro_Sukop.py")
+
+
+def load_grey(ref, p):
+    """The grey-scale script with its parameter lines set to ``p`` and cut
+    before its main loop (``time_init = time.time()``)."""
+    src = open(os.path.join(ref, GREY_FILE)).read()
+    src = src.split("time_init = time.time()")[0]
+    sub = {
+        "nx,ny,nz = 60,50,5\n": "nx,ny,nz = %d,%d,%d\n" % tuple(p["shape"]),
+        "fx,fy,fz = 1.0e-6,0.0,0.0\n": "fx,fy,fz = %r,%r,%r\n" % tuple(p["force"]),
+        "niu = 0.1\n": "niu = %r\n" % p["niu"],
+    }
+    faces = ["x_left", "x_right", "y_left", "y_right", "z_left", "z_right"]
+    short = ["xl", "xr", "yl", "yr", "zl", "zr"]
+    lines = src.splitlines(keepends=True)
+    for line in lines:
+        for fi, (fc, sh) in enumerate(zip(faces, short)):
+            if line.startswith("bc_%s, rho_bc%s" % (fc, sh)):
+                v = p["vel_bc"][fi]
+                sub[line] = "bc_%s, rho_bc%s, vx_bc%s, vy_bc%s, vz_bc%s = %d, %r, %r, %r, %r\n" % (
+                    fc, sh, sh, sh, sh, p["bc"][fi], p["rho_bc"][fi], v[0], v[1], v[2])
+    for a, b in sub.items():
+        hits = [n for n, ln in enumerate(lines) if ln == a]
+        assert len(hits) == 1, a
+        lines[hits[0]] = b
+    g = {"__name__": "ref_lbm_grey"}
+    exec(compile("".join(lines), os.path.join(ref, GREY_FILE), "exec"), g)
+    return g
+
+
+def case_grey(ref, name, p, ns, steps_list):
+    """Run the script's main-loop body (:330-336) and store rho, v after each
+    listed step count.  solid = ns.astype(int) as the script does (:321)."""
+    t0 = time.time()
+    g = load_grey(ref, p)
+    g["solid"].from_numpy(ns.astype(int))
+    g["ns"].from_numpy(ns)
+    g["static_init"]()
+    g["init"]()
+    out = {}
+    done = 0
+    for st in steps_list:
+        while done < st:
+            g["colission"]()
+            g["streaming0"]()
+            g["streaming1"]()
+            g["Boundary_condition"]()
+            g["streaming3"]()
+            done += 1
+        out["rho_%d" % st] = g["rho"].to_numpy().astype(np.float32)
+        out["v_%d" % st] = g["v"].to_numpy().astype(np.float32)
+        out["F_%d" % st] = g["F"].to_numpy().astype(np.float32)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), ns=ns.astype(np.float64), shape=np.array(p["shape"]),
+                        steps=np.array(steps_list), params=json.dumps(p), kind="grey_script", **out)
+    print("%-22s %6.1fs" % (name, time.time() - t0))
+
+
+def grey_params(shape, **kw):
+    p = dict(shape=list(shape), force=[0.0, 0.0, 0.0], niu=0.1, bc=[0] * 6, rho_bc=[1.0] * 6,
+             vel_bc=[[0.0, 0.0, 0.0]] * 6)
+    p.update(kw)
+    return p
+
+
+def gen_grey(ref, only):
+    def want(n):
+        return not only or n in only
+
+    if want("grey_channel"):
+        # channel: ns = 1 walls at y = 0 and y = ny-1, a grey (ns = 0.2) layer
+        # along the lower wall, open fluid above; body force along x
+        shape = (12, 10, 4)
+        ns = np.zeros(shape)
+        ns[:, 0, :] = ns[:, -1, :] = 1.0
+        ns[:, 1:4, :] = 0.2
+        case_grey(ref, "grey_channel", grey_params(shape, force=[1e-4, 0.0, 0.0]), ns, [1, 10])
+
+    if want("grey_mixed"):
+        # seeded random ns in {0, 0.1, 0.2, 0.5, 1}, oblique body force
+        shape = (9, 8, 6)
+        rng = np.random.default_rng(31)
+        ns = rng.choice([0.0, 0.0, 0.0, 0.1, 0.2, 0.5, 1.0], size=shape)
+        case_grey(ref, "grey_mixed", grey_params(shape, force=[2e-5, -1e-5, 5e-6]), ns, [1, 8])
+
+    if want("grey_faces"):
+        # x faces: velocity (in-place form) on the left, pressure on the right;
+        # walls at y = 0 / y = ny-1 reach the faces, so face cells have solid
+        # upstream neighbours
+        shape = (10, 7, 5)
+        rng = np.random.default_rng(32)
+        ns = rng.choice([0.0, 0.0, 0.3, 1.0], size=shape, p=[0.5, 0.2, 0.2, 0.1])
+        ns[:, 0, :] = ns[:, -1, :] = 1.0
+        p = grey_params(shape, bc=[2, 1, 0, 0, 0, 0], rho_bc=[1.0, 0.998, 1.0, 1.0, 1.0, 1.0])
+        case_grey(ref, "grey_faces", p, ns, [1, 6])
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -298,6 +397,7 @@ def main():
     a = ap.parse_args()
     gen_single_phase(a.ref, a.only)
     gen_two_phase(a.ref, a.only)
+    gen_grey(a.ref, a.only)
 
 
 if __name__ == "__main__":

@@ -288,14 +288,16 @@ profiler = _Profiler()
 
 
 def install():
-    """Register this module as ``taichi`` and a no-op ``pyevtk.hl`` in sys.modules."""
+    """Register this module as ``taichi`` and no-op ``pyevtk.hl`` / ``evtk.hl``
+    (the grey-scale script imports the package under its old name) in sys.modules."""
     sys.modules["taichi"] = sys.modules[__name__]
-    pe = types.ModuleType("pyevtk")
-    hl = types.ModuleType("pyevtk.hl")
-    hl.gridToVTK = lambda *a, **k: None
-    pe.hl = hl
-    sys.modules["pyevtk"] = pe
-    sys.modules["pyevtk.hl"] = hl
+    for name in ("pyevtk", "evtk"):
+        pe = types.ModuleType(name)
+        hl = types.ModuleType(name + ".hl")
+        hl.gridToVTK = lambda *a, **k: None
+        pe.hl = hl
+        sys.modules[name] = pe
+        sys.modules[name + ".hl"] = hl
 
 
 def field(dtype, shape=None, **kw):

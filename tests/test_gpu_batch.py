@@ -60,3 +60,30 @@ def test_autotuner_caches(tmp_path):
     assert res2[24]["when"] == res[24]["when"]          # served from the cache
     tiles, block = autotune.plan([24, 16, 24], res)
     assert len(tiles) == 3 and block in autotune.BLOCKS
+
+
+def test_batch_beyond_int32_population_offsets():
+    """A batch whose populations span more than 2^31 elements: three
+    384x384x300 all-fluid subvolumes (132,710,400 nodes, 2.52e9 elements) ahead
+    of a porous one.  The last subvolume's state must match its own single
+    lattice bit for bit, and the uniform ones must stay uniform."""
+    from taichi_lbm3d_gb300.batch import Batch
+    big = np.zeros((384, 384, 300), np.int8)
+    small = sphere_pack((32, 32, 32), 2.5, 5, 0.40, seed=52)
+    b = Batch([big, big, big, small], niu=0.1, force=(1e-5, 0, 0), storage="f16")
+    assert b.info()["nodes"] * 19 > 2 ** 31
+    b.configure([4096, 4096, 4096, 256], 256)
+    b.init()
+    b.step(20, chunk=10)
+    rho_s, v_s = b.macros(3)
+    rho_b, v_b = b.macros(2)
+    b.close()
+    lat = _native.Lattice(_native.make_params(small.shape, niu=0.1, force=(1e-5, 0, 0), visc_convention=1,
+                                              guo_convention=2, storage="f16"))
+    lat.set_geometry(small)
+    lat.init()
+    lat.step(21)            # the macros of step 21 are those of the state the batch holds after 20
+    rho_r, v_r = lat.macros()
+    lat.close()
+    assert np.array_equal(rho_s, rho_r) and np.array_equal(v_s, v_r)
+    assert np.all(rho_b == rho_b.flat[0]) and np.all(v_b[..., 0] == v_b.flat[0]) and v_b.flat[0] > 0

@@ -1,9 +1,9 @@
 """Pin the CPU oracle against outputs of the reference's own kernels.
 
 The fixtures were produced by tests/golden/make_golden.py, which executes
-Single_phase/LBM_3D_SinglePhase_Solver.py and 2phase/lbm_solver_3d_2phase_sparse.py
-unmodified (through a numpy stand-in for Taichi).  Single-phase agreement is
-bit-exact.  Two-phase agreement is bit-exact when the oracle replays the serial
+Single_phase/LBM_3D_SinglePhase_Solver.py, 2phase/lbm_solver_3d_2phase_sparse.py
+and Grey_Scale/lbm_solver_3d_Macro_Sukop.py unmodified (through a numpy
+stand-in for Taichi).  Single-phase and grey-scale agreement is bit-exact.  Two-phase agreement is bit-exact when the oracle replays the serial
 order of the reference's colour push (the reference's own GPU run sums it with
 atomics in no fixed order); in the oracle's deterministic slot order the
 difference is FP32 reordering noise, bounded below.
@@ -113,3 +113,20 @@ def test_fp64_oracle_close_to_fp32():
     fl = d["solid"] == 0
     assert G.normwise_rel(a.field("rho"), b.field("rho"), fl) < 1e-6
     assert G.normwise_rel(a.field("v"), b.field("v"), fl) < 1e-4
+
+
+@pytest.mark.parametrize("name", G.GREY_CASES)
+def test_grey_scale_bit_exact(name):
+    """Partial bounce-back script: rho, v and the full post-stream F (every
+    cell, solid cells included) equal the reference's bit for bit."""
+    d = G.load(name)
+    solid = G.grey_solid(d["ns"])
+    o = Oracle(G.oracle_params(d), solid)
+    o.set_field("ns", d["ns"])
+    done = 0
+    for st in d["steps"]:
+        o.step(int(st) - done)
+        done = int(st)
+        assert np.array_equal(o.field("rho").astype(np.float32), d["rho_%d" % st]), (name, st)
+        assert np.array_equal(o.field("v").astype(np.float32), d["v_%d" % st]), (name, st)
+        assert np.array_equal(o.field("F").astype(np.float32), d["F_%d" % st]), (name, st)
