@@ -1,9 +1,12 @@
 """GPU voxeliser (csrc/vox.cu) against the FP64 CPU oracle.
 
 Flags must agree at every grid point outside a thin band where FP32 and FP64
-can legitimately differ: points within 1e-3 dx of the surface, or whose
-winding number is within 1e-4 of 1/2.  Winding numbers agree to 1e-4 away
-from the surface.
+can legitimately differ: points whose distance to the surface is within a
+factor 2 of the on-surface tolerance (1e-5 dx), or whose winding number is
+within 1e-4 of 1/2 without lying on the surface.  Points exactly on the
+surface (grid planes through a flat cap, for example) are solid in both.
+Winding numbers agree to 1e-4 one cell or more from the surface and to 1e-2
+closer in (FP32 solid angles of nearby triangles lose digits).
 """
 import numpy as np
 import pytest
@@ -29,10 +32,15 @@ def test_gpu_flags_match_oracle(name):
     g_solid, g_w = vx.voxelize(tris, origin, None, dx, dims=dims, with_winding=True)
     o_solid, o_w = oracle.voxelize(tris, origin, dx, dims)
     dist = oracle.mesh_distance(tris, origin, dx, dims)
-    band = (dist < 1e-3 * dx) | (np.abs(np.abs(o_w) - 0.5) < 1e-4)
+    eps = 1e-5 * dx
+    band = (np.abs(dist - eps) < 0.5 * eps) | ((np.abs(np.abs(o_w) - 0.5) < 1e-4) & (dist > 2 * eps))
     assert band.mean() < 1e-3, band.mean()
+    assert np.all(g_solid[dist == 0] == 1) and np.all(o_solid[dist == 0] == 1)
     assert np.array_equal(g_solid[~band], o_solid[~band]), int((g_solid != o_solid)[~band].sum())
-    far = dist > 1e-2 * dx
+    # FP32 solid angles lose digits for triangles close to the point
+    off = dist > 2 * eps
+    assert np.abs(g_w[off] - o_w[off]).max() < 1e-2
+    far = dist > dx
     assert np.abs(g_w[far] - o_w[far]).max() < 1e-4
     assert 0.0 < o_solid.mean() < 1.0
 
