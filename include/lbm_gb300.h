@@ -116,6 +116,11 @@ int lbm_destroy(LbmHandle* h);
  * neighbour map on the device.  The lattice size is the one in LbmParams. */
 int lbm_set_geometry(LbmHandle* h, const int8_t* solid);
 
+/* The same with the mask addressed as solid[i*si + j*sj + k*sk] (element
+ * strides >= 0), e.g. a C-ordered (nx, ny, nz) numpy array without a
+ * transposing copy.  The index is built on the device. */
+int lbm_set_geometry_strided(LbmHandle* h, const int8_t* solid, int64_t si, int64_t sj, int64_t sk);
+
 /* Two-phase initial phase field psi[cell] (TP:195-203, psi.from_numpy). */
 int lbm_set_psi(LbmHandle* h, const float* psi);
 

@@ -62,6 +62,7 @@ SIGNATURES = {
     "lbm_create": [ctypes.POINTER(LbmParams), ctypes.POINTER(_P)],
     "lbm_destroy": [_P],
     "lbm_set_geometry": [_P, _P],
+    "lbm_set_geometry_strided": [_P, _P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64],
     "lbm_set_psi": [_P, _P],
     "lbm_set_grey": [_P, _P],
     "lbm_init": [_P, _P, _P],
@@ -151,10 +152,20 @@ class Lattice:
 
     # --- setup
     def set_geometry(self, solid):
-        s = np.ascontiguousarray(np.asarray(solid).ravel(order="F"), dtype=np.int8)
-        if s.size != self.ncell:
-            raise ValueError("solid has %d cells, lattice has %d" % (s.size, self.ncell))
-        self._c(load().lbm_set_geometry(self.h, ptr(s)))
+        """solid: (nx, ny, nz) array, > 0 solid.  Passed with its own strides
+        (no transposing copy) when it is int8 or bool."""
+        a = np.asarray(solid)
+        if a.shape != self.shape:
+            if a.size != self.ncell:
+                raise ValueError("solid has %d cells, lattice has %d" % (a.size, self.ncell))
+            a = a.reshape(self.shape, order="F")
+        if a.dtype == np.bool_:
+            a = a.view(np.int8)
+        elif a.dtype != np.int8:
+            a = (a > 0).astype(np.int8)
+        if any(st < 0 for st in a.strides):
+            a = np.array(a, order="F")
+        self._c(load().lbm_set_geometry_strided(self.h, ptr(a), *(int(st) for st in a.strides)))
 
     def set_psi(self, psi):
         a = np.ascontiguousarray(np.asarray(psi, dtype=np.float32).ravel(order="F"))

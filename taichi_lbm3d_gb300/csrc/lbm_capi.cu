@@ -180,41 +180,19 @@ int lbm_destroy(LbmHandle* h) {
 }
 
 // Compacted index: fluid nodes in cell order (x fastest), the order in which
-// the reference's block-sparse storage is activated by init (SP:160-170).
-int lbm_set_geometry(LbmHandle* h, const int8_t* solid) {
+// the reference's block-sparse storage is activated by init (SP:160-170);
+// built on the device (lbm_geom.cu).  The mask is addressed as
+// solid[i*si + j*sj + k*sk] (element strides).
+int lbm_set_geometry_strided(LbmHandle* h, const int8_t* solid, int64_t si, int64_t sj, int64_t sk) {
     if (!h || !solid) return lbm_set_err(h, LBM_EINVAL, "lbm_set_geometry: NULL argument");
+    if (si < 0 || sj < 0 || sk < 0) return lbm_set_err(h, LBM_EINVAL, "lbm_set_geometry: negative stride");
     cudaSetDevice(h->device);
     cudaStreamSynchronize(h->stream);
     free_lattice(h);
     h->have_geometry = h->initialized = h->macros_valid = false;
-    const int64_t nc = h->ncell;
-    h->solid.assign(solid, solid + nc);
-    std::vector<int32_t> map(nc);
-    h->cell_of_node.clear();
-    int32_t nf = 0;
-    for (int64_t c = 0; c < nc; ++c) {
-        if (solid[c] > 0) {
-            h->solid[c] = 1;
-            map[c] = -1;
-        } else {
-            h->solid[c] = 0;
-            map[c] = nf++;
-            h->cell_of_node.push_back((int32_t)c);
-        }
-    }
-    h->n_fluid = nf;
-    h->np = ((int64_t)std::max(nf, 1) + 63) / 64 * 64;
-    std::vector<uint32_t> coord(h->np, 0);
-    const int nx = h->p.nx, ny = h->p.ny;
-    for (int32_t n = 0; n < nf; ++n) {
-        const int64_t c = h->cell_of_node[n];
-        const int i = (int)(c % nx), j = (int)((c / nx) % ny), k = (int)(c / ((int64_t)nx * ny));
-        coord[n] = lbm_pack(i, j, k);
-    }
+    int rc = geom_build(h, solid, si, sj, sk);
+    if (rc) { free_lattice(h); return rc; }
     const size_t rbytes = h->f64 ? 8 : 4;
-    int rc = 0;
-    rc = rc ? rc : dev_alloc(h, &h->d_map, sizeof(int32_t) * nc, "map");
-    rc = rc ? rc : dev_alloc(h, &h->d_coord, sizeof(uint32_t) * h->np, "coord");
     rc = rc ? rc : dev_alloc(h, &h->d_f[0], h->elem * 19 * h->np, "f_A");
     rc = rc ? rc : dev_alloc(h, &h->d_f[1], h->elem * 19 * h->np, "f_B");
     rc = rc ? rc : dev_alloc(h, &h->d_vprev, rbytes * 3 * h->np, "vprev");
@@ -236,9 +214,7 @@ int lbm_set_geometry(LbmHandle* h, const int8_t* solid) {
     rc = rc ? rc : dev_alloc(h, &h->d_red, sizeof(double) * 8 * h->red_blocks, "reduction partials");
     rc = rc ? rc : dev_alloc(h, &h->d_red_out, sizeof(double) * 8, "reduction result");
     if (rc) { free_lattice(h); return rc; }
-    rc = lbm_cuda_check(h, cudaMemcpyAsync(h->d_map, map.data(), sizeof(int32_t) * nc, cudaMemcpyHostToDevice, h->stream), "copy map");
-    if (!rc) rc = lbm_cuda_check(h, cudaMemcpyAsync(h->d_coord, coord.data(), sizeof(uint32_t) * h->np, cudaMemcpyHostToDevice, h->stream), "copy coord");
-    if (!rc) rc = lbm_cuda_check(h, cudaMemsetAsync(h->d_f[0], 0, h->elem * 19 * h->np, h->stream), "clear f");
+    rc = lbm_cuda_check(h, cudaMemsetAsync(h->d_f[0], 0, h->elem * 19 * h->np, h->stream), "clear f");
     if (!rc) rc = lbm_cuda_check(h, cudaMemsetAsync(h->d_f[1], 0, h->elem * 19 * h->np, h->stream), "clear f");
     if (!rc) rc = lbm_cuda_check(h, cudaMemsetAsync(h->d_vprev, 0, rbytes * 3 * h->np, h->stream), "clear vprev");
     if (!rc) rc = lbm_cuda_check(h, cudaStreamSynchronize(h->stream), "lbm_set_geometry");
@@ -246,6 +222,11 @@ int lbm_set_geometry(LbmHandle* h, const int8_t* solid) {
     h->have_geometry = true;
     h->have_psi = false;
     return LBM_OK;
+}
+
+int lbm_set_geometry(LbmHandle* h, const int8_t* solid) {
+    if (!h) return lbm_set_err(h, LBM_EINVAL, "lbm_set_geometry: NULL handle");
+    return lbm_set_geometry_strided(h, solid, 1, h->p.nx, (int64_t)h->p.nx * h->p.ny);
 }
 
 // Grey-scale lattice (Grey_Scale/lbm_solver_3d_Macro_Sukop.py): ns per cell,
@@ -264,6 +245,8 @@ int lbm_set_grey(LbmHandle* h, const double* ns) {
     dev_free(h->d_gstale);
     h->grey = false;
     h->initialized = false;
+    int rc = geom_host_index(h);
+    if (rc) return rc;
     const size_t rb = h->f64 ? 8 : 4;
     std::vector<unsigned char> host(rb * h->np, 0);
     for (int32_t n = 0; n < h->n_fluid; ++n) {
@@ -271,7 +254,7 @@ int lbm_set_grey(LbmHandle* h, const double* ns) {
         if (h->f64) ((double*)host.data())[n] = x;
         else ((float*)host.data())[n] = (float)x;
     }
-    int rc = dev_alloc(h, &h->d_ns, rb * h->np, "grey ns");
+    rc = dev_alloc(h, &h->d_ns, rb * h->np, "grey ns");
     if (!rc && (h->p.bc[0] == LBM_BC_VELOCITY || h->p.bc[1] == LBM_BC_VELOCITY))
         rc = dev_alloc(h, &h->d_gstale, rb * 19 * 2 * (size_t)h->p.ny * h->p.nz, "grey face slots");
     if (!rc) rc = lbm_cuda_check(h, cudaMemcpyAsync(h->d_ns, host.data(), host.size(), cudaMemcpyHostToDevice, h->stream), "copy ns");
@@ -312,6 +295,8 @@ int lbm_init(LbmHandle* h, const float* rho, const float* v) {
         float* d_in = nullptr;
         if (rho) {
             // gather the dense fields into node order: rho [np], v [3][np]
+            rc = geom_host_index(h);
+            if (rc) return rc;
             std::vector<float> hin(4 * h->np, 0.0f);
             for (int32_t n = 0; n < h->n_fluid; ++n) {
                 const int64_t c = h->cell_of_node[n];
@@ -380,23 +365,10 @@ int lbm_get_stream(LbmHandle* h, void** stream) {
 namespace {
 // Copy a node-ordered device array (n components of stride np, FP32 or FP64)
 // into a dense host array with `comps` interleaved components; solid cells get
-// `fill`.
+// `fill` (scattered on the device, lbm_geom.cu).
 template <typename O>
 int scatter_dense(LbmHandle* h, const void* dsrc, int comps, O* out, O fill) {
-    const size_t rb = h->f64 ? 8 : 4;
-    std::vector<unsigned char> tmp(rb * comps * h->np);
-    int rc = lbm_cuda_check(h, cudaMemcpyAsync(tmp.data(), dsrc, tmp.size(), cudaMemcpyDeviceToHost, h->stream), "copy out");
-    if (!rc) rc = lbm_cuda_check(h, cudaStreamSynchronize(h->stream), "copy out");
-    if (rc) return rc;
-    for (int64_t c = 0; c < h->ncell * comps; ++c) out[c] = fill;
-    for (int32_t n = 0; n < h->n_fluid; ++n) {
-        const int64_t c = h->cell_of_node[n];
-        for (int d = 0; d < comps; ++d) {
-            const int64_t idx = (int64_t)d * h->np + n;
-            out[c * comps + d] = h->f64 ? (O)((const double*)tmp.data())[idx] : (O)((const float*)tmp.data())[idx];
-        }
-    }
-    return LBM_OK;
+    return geom_dense_out<O>(h, dsrc, comps, out, fill);
 }
 }  // namespace
 
@@ -442,7 +414,8 @@ int lbm_get_phase(LbmHandle* h, float* psi, float* rho_r, float* rho_b) {
     if (psi) {
         // fluid cells from the device; solid cells keep the input psi (the reference never updates them)
         std::vector<float> fl(h->ncell);
-        rc = scatter_dense<float>(h, h->d_psi, 1, fl.data(), 0.0f);
+        rc = geom_host_index(h);
+        if (!rc) rc = scatter_dense<float>(h, h->d_psi, 1, fl.data(), 0.0f);
         if (!rc)
             for (int64_t c = 0; c < h->ncell; ++c) psi[c] = h->solid[c] ? h->psi0[c] : fl[c];
     }
@@ -528,6 +501,9 @@ int lbm_get_info(LbmHandle* h, LbmInfo* out) {
 int lbm_get_fluid_index(LbmHandle* h, int32_t* cell_of_node) {
     if (!h || !cell_of_node) return lbm_set_err(h, LBM_EINVAL, "lbm_get_fluid_index: NULL argument");
     if (!h->have_geometry) return lbm_set_err(h, LBM_ESTATE, "lbm_get_fluid_index: no geometry");
+    cudaSetDevice(h->device);
+    const int rc = geom_host_index(h);
+    if (rc) return rc;
     std::memcpy(cell_of_node, h->cell_of_node.data(), sizeof(int32_t) * h->n_fluid);
     return LBM_OK;
 }
@@ -536,8 +512,11 @@ int lbm_get_neighbors(LbmHandle* h, int32_t* src) {
     if (!h || !src) return lbm_set_err(h, LBM_EINVAL, "lbm_get_neighbors: NULL argument");
     if (!h->have_geometry) return lbm_set_err(h, LBM_ESTATE, "lbm_get_neighbors: no geometry");
     // Read the map back from the device: the table is what the kernels use.
+    cudaSetDevice(h->device);
+    int rc = geom_host_index(h);
+    if (rc) return rc;
     std::vector<int32_t> map(h->ncell);
-    int rc = lbm_cuda_check(h, cudaMemcpy(map.data(), h->d_map, sizeof(int32_t) * h->ncell, cudaMemcpyDeviceToHost), "copy map");
+    rc = lbm_cuda_check(h, cudaMemcpy(map.data(), h->d_map, sizeof(int32_t) * h->ncell, cudaMemcpyDeviceToHost), "copy map");
     if (rc) return rc;
     const int nx = h->p.nx, ny = h->p.ny, nz = h->p.nz;
     for (int32_t n = 0; n < h->n_fluid; ++n) {

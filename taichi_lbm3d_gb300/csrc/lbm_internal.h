@@ -42,8 +42,9 @@ struct LbmHandle {
     bool f64 = false;         // compute in FP64
     bool force = false;
 
-    std::vector<int8_t> solid;             // dense host copy
-    std::vector<int32_t> cell_of_node;     // n_fluid
+    std::vector<int8_t> solid;             // dense host copy (made on demand: geom_host_index)
+    std::vector<int32_t> cell_of_node;     // n_fluid (made on demand)
+    bool host_index_valid = false;
     std::vector<float> psi0;               // dense initial psi (two phase)
 
     int32_t* d_map = nullptr;              // dense: node index or -1 (solid)
@@ -74,6 +75,12 @@ struct LbmHandle {
 
 int lbm_set_err(LbmHandle* h, int code, const std::string& msg);
 int lbm_cuda_check(LbmHandle* h, cudaError_t e, const char* what);
+
+// index construction and dense output (lbm_geom.cu)
+int geom_build(LbmHandle* h, const int8_t* solid, int64_t si, int64_t sj, int64_t sk);
+int geom_host_index(LbmHandle* h);
+template <typename O>
+int geom_dense_out(LbmHandle* h, const void* dsrc, int comps, O* out, O fill);
 
 // single phase (lbm_sp.cu)
 int sp_launch_init(LbmHandle* h, const void* rho_nodes, const void* v_nodes);

@@ -407,9 +407,11 @@ int tp_init_t(LbmHandle* h) {
     using Tt = typename Codec<STORE>::T;
     const TpConsts<R> T = make_tp<R>(h);
     // psi of the fluid nodes, in node order
+    int rc = geom_host_index(h);
+    if (rc) return rc;
     std::vector<R> hp(h->np, (R)0);
     for (int32_t n = 0; n < h->n_fluid; ++n) hp[n] = (R)h->psi0[h->cell_of_node[n]];
-    int rc = lbm_cuda_check(h, cudaMemcpyAsync(h->d_psi, hp.data(), sizeof(R) * h->np, cudaMemcpyHostToDevice, h->stream),
+    rc = lbm_cuda_check(h, cudaMemcpyAsync(h->d_psi, hp.data(), sizeof(R) * h->np, cudaMemcpyHostToDevice, h->stream),
                             "copy psi");
     if (rc) return rc;
     h->cur = 0;
