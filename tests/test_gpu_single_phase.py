@@ -235,3 +235,33 @@ def test_errors_are_reported():
     lat = _native.Lattice(_native.make_params((8, 8, 8)))
     with pytest.raises(_native.LbmError):
         lat.step(1)          # before geometry / init
+
+
+def test_strided_geometry_gives_the_same_index():
+    """The device-built index does not depend on the mask's memory layout
+    (C order, Fortran order, a bool view, a non-contiguous slice)."""
+    solid = sphere_pack((30, 22, 17), 2.0, 4.0, 0.45, seed=12)
+    ref = None
+    big = np.zeros((60, 22, 17), np.int8)
+    big[::2] = solid
+    for arr in (solid, np.asfortranarray(solid), solid.astype(bool), big[::2], solid.astype(np.int32)):
+        lat = _native.Lattice(_native.make_params(solid.shape))
+        lat.set_geometry(arr)
+        idx = lat.fluid_index()
+        nb = lat.neighbors()
+        lat.close()
+        if ref is None:
+            ref = (idx, nb)
+            cells = np.nonzero(solid.ravel(order="F") == 0)[0]
+            assert np.array_equal(idx, cells)
+        else:
+            assert np.array_equal(idx, ref[0]) and np.array_equal(nb, ref[1])
+
+
+def test_too_many_fluid_nodes_for_one_lattice_is_an_error():
+    # 512 x 512 x 440 all fluid = 115,343,360 nodes > 2^31 / 19
+    lat = _native.Lattice(_native.make_params((512, 512, 440)))
+    with pytest.raises(_native.LbmError) as ei:
+        lat.set_geometry(np.zeros((512, 512, 440), np.int8))
+    assert "fluid nodes" in str(ei.value)
+    lat.close()
