@@ -24,6 +24,14 @@ extern "C" {
  * voxels and cin multiples of 16; cout in {16, 32, 48, 64, 96}. */
 int lbm_nn_conv3d(const void* in, const void* w, const float* bias, const void* mask, void* out, int32_t n, int32_t d,
                   int32_t h, int32_t wd, int32_t cin, int32_t cout, int32_t mode, void* stream);
+/* The same convolution on the 5th-generation tensor cores (tcgen05.mma with a
+ * tensor-memory accumulator, 128 voxels per CTA); any voxel count, cin a
+ * multiple of 16 up to 128. */
+int lbm_nn_conv3d_tc(const void* in, const void* w, const float* bias, const void* mask, void* out, int32_t n,
+                     int32_t d, int32_t h, int32_t wd, int32_t cin, int32_t cout, int32_t mode, void* stream);
+/* *timed_out = 1 when a tensor-core convolution gave up waiting on its
+ * pipeline since the last call (its output is then invalid); clears the flag. */
+int lbm_nn_tc_status(int32_t* timed_out);
 /* wt[ci][tap][co] = w[co][26 - tap][ci]: weights of the backward-data conv. */
 int lbm_nn_flip_transpose(const void* w, void* wt, int32_t cin, int32_t cout, void* stream);
 /* Weight gradient dw[co][tap][ci] (FP32) and bias gradient db[co] (may be NULL)

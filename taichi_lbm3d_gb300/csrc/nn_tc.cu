@@ -1,0 +1,288 @@
+// 3x3x3 convolution of the warm-start network on the 5th-generation tensor
+// cores: tcgen05.mma (BF16 x BF16 -> FP32) with the accumulator in tensor
+// memory.  Implicit GEMM: M = 128 consecutive voxels per CTA (one TMEM lane
+// each), N = output channels (16..96), K = 27 taps x input channels.
+//
+// Per tap (one pipeline stage): each of the 128 threads gathers its voxel's
+// shifted input row (cin BF16 values, zero for taps outside the volume) with
+// 16-byte cp.async copies into the canonical K-major layout of the MMA operand
+// (8-row x 16-byte core matrices; LBO = 128 B between the two core matrices of
+// a 16-channel K step, SBO = 256 B between 8-row groups), and the weights of
+// that tap the same way; then one elected thread issues cin/16 MMAs of
+// K = 16 and commits them to the stage's mbarrier.  Three stages let the loads
+// of the next taps run while the tensor core works.  After the last tap the
+// accumulator is read back with tcgen05.ld (warp w owns lanes 32w..32w+31),
+// and the epilogue applies bias + ReLU (forward) or the ReLU mask of the layer
+// input (backward data) and stores BF16.
+//
+// Every wait on an mbarrier is bounded (about a second of clock cycles); on a
+// timeout the CTA records an error flag, waits (bounded) for its own MMAs,
+// frees its tensor memory and exits.  lbm_nn_tc_status reads the flag.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/lbm_nn.h"
+#include "lbm_internal.h"
+
+namespace {
+typedef __nv_bfloat16 bf16;
+
+constexpr int TC_M = 128;
+constexpr int TC_THREADS = 128;
+constexpr int TC_STAGES = 3;
+constexpr long long TC_WAIT_CYCLES = 2000000000LL;   // about 1 s at 2 GHz
+
+__device__ int g_tc_error;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+// Wait for the phase with the given parity to complete; false after ~1 s.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    const long long t0 = clock64();
+    for (;;) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(smem_u32(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (clock64() - t0 > TC_WAIT_CYCLES) return false;
+    }
+}
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, bool valid) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(valid ? 16 : 0) : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major, no swizzle.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((addr >> 4) & 0x3FFF);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+    d |= (uint64_t)1 << 46;   // fixed 0b001 at bits 46-48
+    return d;                  // base offset 0, swizzle mode 0 (none)
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulate, BF16 A and B, both K-major.
+__host__ __device__ constexpr uint32_t mma_idesc(int m, int n) {
+    return (1u << 4)                       // D: F32
+           | (1u << 7)                     // A: BF16
+           | (1u << 10)                    // B: BF16
+           | ((uint32_t)(n >> 3) << 17)    // N / 8
+           | ((uint32_t)(m >> 4) << 24);   // M / 16
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t taddr, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t accum) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(taddr),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accum)
+        : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float* v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int q = 0; q < 16; ++q) v[q] = __uint_as_float(r[q]);
+}
+
+// Byte offset of (row, 8-element chunk h) of a K = 16 step in the canonical layout.
+__device__ __forceinline__ uint32_t canon(int row, int h) { return (uint32_t)((row >> 3) * 256 + h * 128 + (row & 7) * 16); }
+
+template <int COUT, int MODE>
+__global__ void __launch_bounds__(TC_THREADS) conv3d_tc_kernel(const bf16* __restrict__ in, const bf16* __restrict__ w,
+                                                              const float* __restrict__ bias,
+                                                              const bf16* __restrict__ mask, bf16* __restrict__ out,
+                                                              int N, int D, int H, int W, int cin) {
+    constexpr uint32_t NCOL = COUT <= 32 ? 32 : (COUT <= 64 ? 64 : 128);
+    constexpr uint32_t IDESC = mma_idesc(TC_M, COUT);
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ uint64_t s_bar[TC_STAGES + 1];   // per-stage "consumed" + final "done"
+    __shared__ uint32_t s_taddr;
+    __shared__ int s_fail;
+
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int kc = cin >> 4;                              // K steps of 16 channels per tap
+    const uint32_t a_bytes = (uint32_t)kc * 4096u;        // 128 rows x 32 B per K step
+    const uint32_t b_bytes = (uint32_t)kc * COUT * 32u;
+    const uint32_t stage_bytes = a_bytes + b_bytes;
+    const uint32_t smem0 = smem_u32(smem);
+
+    if (tid == 0) {
+        for (int s = 0; s <= TC_STAGES; ++s) mbar_init(&s_bar[s], 1);
+        s_fail = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&s_taddr)),
+                     "r"(NCOL)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t taddr = s_taddr;
+
+    // this thread's output voxel (row of the tile)
+    const int64_t nvox = (int64_t)N * D * H * W;
+    const int64_t v = (int64_t)blockIdx.x * TC_M + tid;
+    const bool live = v < nvox;
+    int x = 0, y = 0, z = 0, n = 0;
+    if (live) {
+        x = (int)(v % W);
+        int64_t t = v / W;
+        y = (int)(t % H);
+        t /= H;
+        z = (int)(t % D);
+        n = (int)(t / D);
+    }
+
+    bool ok = true;
+    for (int tap = 0; tap < 27 && ok; ++tap) {
+        const int s = tap % TC_STAGES;
+        if (tap >= TC_STAGES) {
+            // the MMAs that last read this stage have completed
+            if (!mbar_wait(&s_bar[s], (uint32_t)((tap / TC_STAGES - 1) & 1))) s_fail = 1;
+            __syncthreads();
+            if (s_fail) { ok = false; break; }
+        }
+        const uint32_t sa = smem0 + (uint32_t)s * stage_bytes;
+        const uint32_t sb = sa + a_bytes;
+        // A: the shifted input row of this thread's voxel
+        const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+        const int zz = z + dz, yy = y + dy, xx = x + dx;
+        const bool in_range = live && zz >= 0 && zz < D && yy >= 0 && yy < H && xx >= 0 && xx < W;
+        const bf16* src = in_range ? in + ((((int64_t)n * D + zz) * H + yy) * W + xx) * cin : in;
+        for (int ks = 0; ks < kc; ++ks) {
+            cp_async16(sa + (uint32_t)ks * 4096u + canon(tid, 0), src + ks * 16, in_range);
+            cp_async16(sa + (uint32_t)ks * 4096u + canon(tid, 1), src + ks * 16 + 8, in_range);
+        }
+        // B: weights of this tap, w[co][tap][ci] (row co, K = ci)
+        for (int e = tid; e < COUT * kc * 2; e += TC_THREADS) {
+            const int co = e / (kc * 2), rem = e % (kc * 2), ks = rem >> 1, h = rem & 1;
+            const bf16* wsrc = w + ((int64_t)co * 27 + tap) * cin + ks * 16 + h * 8;
+            cp_async16(sb + (uint32_t)ks * (COUT * 32u) + canon(co, h), wsrc, true);
+        }
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            for (int ks = 0; ks < kc; ++ks) {
+                const uint64_t ad = smem_desc(sa + (uint32_t)ks * 4096u, 128, 256);
+                const uint64_t bd = smem_desc(sb + (uint32_t)ks * (COUT * 32u), 128, 256);
+                tc_mma(taddr, ad, bd, IDESC, (tap > 0 || ks > 0) ? 1u : 0u);
+            }
+            tc_commit(&s_bar[s]);
+        }
+    }
+    // all MMAs issued so far complete -> "done"
+    if (tid == 0) tc_commit(&s_bar[TC_STAGES]);
+    const bool done = mbar_wait(&s_bar[TC_STAGES], 0);
+    if (!done) s_fail = 1;
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (!s_fail) {
+        const uint32_t tw = taddr + ((uint32_t)(warp * 32) << 16);   // this warp's 32 lanes
+#pragma unroll
+        for (int c0 = 0; c0 < COUT; c0 += 16) {
+            float acc[16];
+            tc_ld16(tw + (uint32_t)c0, acc);
+            if (live) {
+                __align__(16) bf16 o[16];
+#pragma unroll
+                for (int q = 0; q < 16; ++q) {
+                    float r = acc[q];
+                    if constexpr (MODE == 0) {
+                        r = fmaxf(r + (bias ? bias[c0 + q] : 0.f), 0.f);
+                    } else {
+                        if (mask && !(__bfloat162float(mask[v * COUT + c0 + q]) > 0.f)) r = 0.f;
+                    }
+                    o[q] = __float2bfloat16_rn(r);
+                }
+                uint4* dst = reinterpret_cast<uint4*>(out + v * COUT + c0);
+                dst[0] = reinterpret_cast<const uint4*>(o)[0];
+                dst[1] = reinterpret_cast<const uint4*>(o)[1];
+            }
+        }
+    } else if (tid == 0) {
+        atomicExch(&g_tc_error, 1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(NCOL) : "memory");
+}
+
+template <int COUT, int MODE>
+int launch_tc(const bf16* in, const bf16* w, const float* bias, const bf16* mask, bf16* out, int n, int d, int h,
+              int wd, int cin, cudaStream_t s) {
+    const int kc = cin / 16;
+    const size_t smem = (size_t)TC_STAGES * ((size_t)kc * 4096 + (size_t)kc * COUT * 32);
+    auto k = conv3d_tc_kernel<COUT, MODE>;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return lbm_set_err(nullptr, LBM_ECUDA, "lbm_nn_conv3d: shared memory attribute");
+    const int64_t nvox = (int64_t)n * d * h * wd;
+    const int grid = (int)((nvox + TC_M - 1) / TC_M);
+    k<<<grid, TC_THREADS, smem, s>>>(in, w, bias, mask, out, n, d, h, wd, cin);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return lbm_set_err(nullptr, LBM_ECUDA, std::string("conv3d_tc_kernel: ") + cudaGetErrorString(e));
+    return LBM_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int lbm_nn_conv3d_tc(const void* in, const void* w, const float* bias, const void* mask, void* out, int32_t n,
+                     int32_t d, int32_t h, int32_t wd, int32_t cin, int32_t cout, int32_t mode, void* stream) {
+    const int64_t nvox = (int64_t)n * d * h * wd;
+    if (!in || !w || !out || nvox <= 0 || cin % 16 || cin <= 0 || cin > 128 || (mode != 0 && mode != 1))
+        return lbm_set_err(nullptr, LBM_EINVAL, "lbm_nn_conv3d: cin must be a multiple of 16 in [16, 128]; mode 0 or 1");
+    cudaStream_t s = (cudaStream_t)stream;
+    const bf16* I = (const bf16*)in;
+    const bf16* Wt = (const bf16*)w;
+    const bf16* M = (const bf16*)mask;
+    bf16* O = (bf16*)out;
+#define LBM_TC(C)                                                                               \
+    case C:                                                                                     \
+        return mode == 0 ? launch_tc<C, 0>(I, Wt, bias, M, O, n, d, h, wd, cin, s)              \
+                         : launch_tc<C, 1>(I, Wt, bias, M, O, n, d, h, wd, cin, s);
+    switch (cout) {
+        LBM_TC(16) LBM_TC(32) LBM_TC(48) LBM_TC(64) LBM_TC(96)
+    default:
+        return lbm_set_err(nullptr, LBM_EINVAL, "lbm_nn_conv3d: cout must be 16, 32, 48, 64 or 96");
+    }
+#undef LBM_TC
+}
+
+// 0 when no tensor-core convolution has timed out since the last call; clears the flag.
+int lbm_nn_tc_status(int32_t* timed_out) {
+    if (!timed_out) return lbm_set_err(nullptr, LBM_EINVAL, "lbm_nn_tc_status: NULL");
+    int v = 0, zero = 0;
+    if (cudaMemcpyFromSymbol(&v, g_tc_error, sizeof(int)) != cudaSuccess ||
+        cudaMemcpyToSymbol(g_tc_error, &zero, sizeof(int)) != cudaSuccess)
+        return lbm_set_err(nullptr, LBM_ECUDA, "lbm_nn_tc_status: symbol copy failed");
+    *timed_out = v;
+    return LBM_OK;
+}
+
+}  // extern "C"

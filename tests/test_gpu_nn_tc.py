@@ -1,0 +1,49 @@
+"""Tensor-core (tcgen05) 3x3x3 convolution against an FP64 numpy reference
+and against the mma.sync kernel, for the channel counts of the network, both
+modes, and voxel counts that leave a partial 128-voxel tile."""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [(16, 16), (16, 32), (32, 32), (32, 64), (64, 64), (96, 32), (48, 16), (32, 96), (16, 48), (64, 32)]
+
+
+def ref_conv(x, w, b, mask, mode):
+    """x (D,H,W,cin), w (cout,27,cin); FP64."""
+    from oracle.unet_oracle import conv_fwd
+    y = conv_fwd(x, w, np.zeros(w.shape[0]) if b is None else b)
+    if mode == 0:
+        return np.maximum(y, 0.0)
+    return y if mask is None else y * (mask > 0)
+
+
+@pytest.mark.parametrize("cin,cout", SHAPES)
+@pytest.mark.parametrize("mode", [0, 1])
+def test_tc_conv_matches_reference(cin, cout, mode):
+    import torch
+    from taichi_lbm3d_gb300 import unet
+    L = unet._lib()
+    rng = np.random.default_rng(cin * 131 + cout + mode)
+    D, H, W = 5, 7, 11                       # 385 voxels: three full tiles and a partial one
+    x = torch.from_numpy(rng.standard_normal((1, D, H, W, cin)).astype(np.float32)).to(torch.bfloat16)
+    w = torch.from_numpy((rng.standard_normal((cout, 27, cin)) / np.sqrt(27 * cin)).astype(np.float32)).to(torch.bfloat16)
+    b = torch.from_numpy(rng.standard_normal(cout).astype(np.float32) * 0.1)
+    m = torch.from_numpy(rng.standard_normal((1, D, H, W, cout)).astype(np.float32)).to(torch.bfloat16)
+    xg, wg, bg, mg = x.cuda().contiguous(), w.cuda().contiguous(), b.cuda(), m.cuda().contiguous()
+    out_tc = torch.zeros((1, D, H, W, cout), dtype=torch.bfloat16, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    rc = L.lbm_nn_conv3d_tc(p(xg), p(wg), p(bg) if mode == 0 else None, p(mg) if mode == 1 else None, p(out_tc),
+                            1, D, H, W, cin, cout, mode, ctypes.c_void_p(s))
+    assert rc == 0
+    torch.cuda.synchronize()
+    flag = ctypes.c_int32(7)
+    assert L.lbm_nn_tc_status(ctypes.byref(flag)) == 0 and flag.value == 0
+    y = out_tc.float().cpu().numpy()[0].astype(np.float64)
+    r = ref_conv(x.float().numpy()[0].astype(np.float64), w.float().numpy().astype(np.float64),
+                 b.numpy().astype(np.float64) if mode == 0 else None, m.float().numpy()[0], mode)
+    err = np.abs(y - r).max() / max(np.abs(r).max(), 1e-30)
+    assert err < 1e-2, err
