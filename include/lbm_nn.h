@@ -18,17 +18,13 @@
 extern "C" {
 #endif
 
-/* 3x3x3 convolution, zero padding, tensor-core implicit GEMM.  mode 0:
+/* 3x3x3 convolution, zero padding, implicit GEMM on the tcgen05 tensor cores
+ * (accumulator in tensor memory, 128 voxels per CTA).  mode 0:
  * out = relu(conv(in, w) + bias); mode 1: out = conv(in, w) * (mask > 0)
  * (mask NULL: no mask) -- the backward-data pass with flip-transposed weights.
- * voxels and cin multiples of 16; cout in {16, 32, 48, 64, 96}. */
+ * Any voxel count; cin a multiple of 16 up to 128; cout in {16, 32, 48, 64, 96}. */
 int lbm_nn_conv3d(const void* in, const void* w, const float* bias, const void* mask, void* out, int32_t n, int32_t d,
                   int32_t h, int32_t wd, int32_t cin, int32_t cout, int32_t mode, void* stream);
-/* The same convolution on the 5th-generation tensor cores (tcgen05.mma with a
- * tensor-memory accumulator, 128 voxels per CTA); any voxel count, cin a
- * multiple of 16 up to 128. */
-int lbm_nn_conv3d_tc(const void* in, const void* w, const float* bias, const void* mask, void* out, int32_t n,
-                     int32_t d, int32_t h, int32_t wd, int32_t cin, int32_t cout, int32_t mode, void* stream);
 /* *timed_out = 1 when a tensor-core convolution gave up waiting on its
  * pipeline since the last call (its output is then invalid); clears the flag. */
 int lbm_nn_tc_status(int32_t* timed_out);

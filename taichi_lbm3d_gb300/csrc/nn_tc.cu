@@ -3,17 +3,19 @@
 // memory.  Implicit GEMM: M = 128 consecutive voxels per CTA (one TMEM lane
 // each), N = output channels (16..96), K = 27 taps x input channels.
 //
-// Per tap (one pipeline stage): each of the 128 threads gathers its voxel's
-// shifted input row (cin BF16 values, zero for taps outside the volume) with
-// 16-byte cp.async copies into the canonical K-major layout of the MMA operand
-// (8-row x 16-byte core matrices; LBO = 128 B between the two core matrices of
-// a 16-channel K step, SBO = 256 B between 8-row groups), and the weights of
-// that tap the same way; then one elected thread issues cin/16 MMAs of
-// K = 16 and commits them to the stage's mbarrier.  Three stages let the loads
-// of the next taps run while the tensor core works.  After the last tap the
-// accumulator is read back with tcgen05.ld (warp w owns lanes 32w..32w+31),
-// and the epilogue applies bias + ReLU (forward) or the ReLU mask of the layer
-// input (backward data) and stores BF16.
+// Per K step of 16 channels of one tap (one pipeline stage): each of the 128
+// threads gathers 32 bytes of its voxel's shifted input row (zero for taps
+// outside the volume) with 16-byte cp.async copies into the canonical K-major
+// layout of the MMA operand (8-row x 16-byte core matrices; LBO = 128 B between
+// the two core matrices of the K step, SBO = 256 B between 8-row groups), and
+// the weights of that step the same way; then one elected thread issues the
+// K = 16 MMA and commits it to the stage's mbarrier.  Eight stages of 5-7 KB:
+// the copies of the next six steps are in flight while the current one is
+// multiplied, a stage is refilled two steps after its MMA was issued, and
+// several CTAs share an SM.
+// After the last tap the accumulator is read back with tcgen05.ld (warp w owns
+// lanes 32w..32w+31), and the epilogue applies bias + ReLU (forward) or the
+// ReLU mask of the layer input (backward data) and stores BF16.
 //
 // Every wait on an mbarrier is bounded (about a second of clock cycles); on a
 // timeout the CTA records an error flag, waits (bounded) for its own MMAs,
@@ -30,7 +32,8 @@ typedef __nv_bfloat16 bf16;
 
 constexpr int TC_M = 128;
 constexpr int TC_THREADS = 128;
-constexpr int TC_STAGES = 3;
+constexpr int TC_STAGES = 8;
+constexpr int TC_AHEAD = 6;    // K steps whose copies are in flight ahead of the one multiplied
 constexpr long long TC_WAIT_CYCLES = 2000000000LL;   // about 1 s at 2 GHz
 
 __device__ int g_tc_error;
@@ -56,8 +59,8 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
     }
 }
 
-__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, bool valid) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(valid ? 16 : 0) : "memory");
+__device__ __forceinline__ void cp_async16_ca(uint32_t dst, const void* src, bool valid) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(valid ? 16 : 0) : "memory");
 }
 
 // Shared-memory matrix descriptor: K-major, no swizzle.
@@ -121,9 +124,7 @@ __global__ void __launch_bounds__(TC_THREADS) conv3d_tc_kernel(const bf16* __res
 
     const int tid = threadIdx.x, warp = tid >> 5;
     const int kc = cin >> 4;                              // K steps of 16 channels per tap
-    const uint32_t a_bytes = (uint32_t)kc * 4096u;        // 128 rows x 32 B per K step
-    const uint32_t b_bytes = (uint32_t)kc * COUT * 32u;
-    const uint32_t stage_bytes = a_bytes + b_bytes;
+    const uint32_t stage_bytes = 4096u + COUT * 32u;      // A: 128 rows x 32 B, B: COUT rows x 32 B
     const uint32_t smem0 = smem_u32(smem);
 
     if (tid == 0) {
@@ -156,45 +157,62 @@ __global__ void __launch_bounds__(TC_THREADS) conv3d_tc_kernel(const bf16* __res
         n = (int)(t / D);
     }
 
-    bool ok = true;
-    for (int tap = 0; tap < 27 && ok; ++tap) {
-        const int s = tap % TC_STAGES;
-        if (tap >= TC_STAGES) {
-            // the MMAs that last read this stage have completed
-            if (!mbar_wait(&s_bar[s], (uint32_t)((tap / TC_STAGES - 1) & 1))) s_fail = 1;
-            __syncthreads();
-            if (s_fail) { ok = false; break; }
-        }
+    // gather K step q (tap q / kc, channels 16 (q % kc) .. +15) into stage s:
+    // A = this thread's shifted input row (zero outside the volume),
+    // B = w[co][tap][ci] (row co, K = ci).  cp.async.ca keeps the input rows in
+    // L1, where the 27 taps of neighbouring voxels find them again.
+    auto load_step = [&](int q, int s) {
+        const int tap = q / kc, ks = q - tap * kc;
         const uint32_t sa = smem0 + (uint32_t)s * stage_bytes;
-        const uint32_t sb = sa + a_bytes;
-        // A: the shifted input row of this thread's voxel
+        const uint32_t sb = sa + 4096u;
         const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
         const int zz = z + dz, yy = y + dy, xx = x + dx;
         const bool in_range = live && zz >= 0 && zz < D && yy >= 0 && yy < H && xx >= 0 && xx < W;
-        const bf16* src = in_range ? in + ((((int64_t)n * D + zz) * H + yy) * W + xx) * cin : in;
-        for (int ks = 0; ks < kc; ++ks) {
-            cp_async16(sa + (uint32_t)ks * 4096u + canon(tid, 0), src + ks * 16, in_range);
-            cp_async16(sa + (uint32_t)ks * 4096u + canon(tid, 1), src + ks * 16 + 8, in_range);
+        const bf16* src = in_range ? in + ((((int64_t)n * D + zz) * H + yy) * W + xx) * cin + ks * 16 : in;
+        cp_async16_ca(sa + canon(tid, 0), src, in_range);
+        cp_async16_ca(sa + canon(tid, 1), src + 8, in_range);
+        for (int e = tid; e < COUT * 2; e += TC_THREADS) {
+            const int co = e >> 1, h = e & 1;
+            cp_async16_ca(sb + canon(co, h), w + ((int64_t)co * 27 + tap) * cin + ks * 16 + h * 8, true);
         }
-        // B: weights of this tap, w[co][tap][ci] (row co, K = ci)
-        for (int e = tid; e < COUT * kc * 2; e += TC_THREADS) {
-            const int co = e / (kc * 2), rem = e % (kc * 2), ks = rem >> 1, h = rem & 1;
-            const bf16* wsrc = w + ((int64_t)co * 27 + tap) * cin + ks * 16 + h * 8;
-            cp_async16(sb + (uint32_t)ks * (COUT * 32u) + canon(co, h), wsrc, true);
+    };
+
+    // K steps run through TC_STAGES stages; the copies of the next TC_AHEAD
+    // steps are in flight while the current one is multiplied, and a stage is
+    // refilled TC_STAGES - TC_AHEAD steps after its MMA was issued, so that
+    // MMA has normally finished by then.
+    const int nq = 27 * kc;
+#pragma unroll 1
+    for (int q = 0; q < TC_AHEAD; ++q) {
+        if (q < nq) load_step(q, q);
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    }
+#pragma unroll 1
+    for (int q = 0; q < nq; ++q) {
+        const int qn = q + TC_AHEAD;   // step to prefetch
+        if (qn < nq) {
+            const int sn = qn % TC_STAGES;
+            if (qn >= TC_STAGES) {
+                // the MMA of step qn - TC_STAGES, which read stage sn, has completed
+                if (!mbar_wait(&s_bar[sn], (uint32_t)((qn / TC_STAGES - 1) & 1))) s_fail = 1;
+                __syncthreads();
+                if (s_fail) break;
+            }
+            load_step(qn, sn);
         }
-        asm volatile("cp.async.wait_all;" ::: "memory");
+        asm volatile("cp.async.commit_group;" ::: "memory");
+        asm volatile("cp.async.wait_group %0;" ::"n"(TC_AHEAD) : "memory");   // step q's copies are complete
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
         if (tid == 0) {
+            const int s = q % TC_STAGES;
+            const uint32_t sa = smem0 + (uint32_t)s * stage_bytes;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            for (int ks = 0; ks < kc; ++ks) {
-                const uint64_t ad = smem_desc(sa + (uint32_t)ks * 4096u, 128, 256);
-                const uint64_t bd = smem_desc(sb + (uint32_t)ks * (COUT * 32u), 128, 256);
-                tc_mma(taddr, ad, bd, IDESC, (tap > 0 || ks > 0) ? 1u : 0u);
-            }
+            tc_mma(taddr, smem_desc(sa, 128, 256), smem_desc(sa + 4096u, 128, 256), IDESC, q > 0 ? 1u : 0u);
             tc_commit(&s_bar[s]);
         }
     }
+    asm volatile("cp.async.wait_all;" ::: "memory");   // no copies left in flight on any path
     // all MMAs issued so far complete -> "done"
     if (tid == 0) tc_commit(&s_bar[TC_STAGES]);
     const bool done = mbar_wait(&s_bar[TC_STAGES], 0);
@@ -236,8 +254,7 @@ __global__ void __launch_bounds__(TC_THREADS) conv3d_tc_kernel(const bf16* __res
 template <int COUT, int MODE>
 int launch_tc(const bf16* in, const bf16* w, const float* bias, const bf16* mask, bf16* out, int n, int d, int h,
               int wd, int cin, cudaStream_t s) {
-    const int kc = cin / 16;
-    const size_t smem = (size_t)TC_STAGES * ((size_t)kc * 4096 + (size_t)kc * COUT * 32);
+    const size_t smem = (size_t)TC_STAGES * (4096 + (size_t)COUT * 32);
     auto k = conv3d_tc_kernel<COUT, MODE>;
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return lbm_set_err(nullptr, LBM_ECUDA, "lbm_nn_conv3d: shared memory attribute");
@@ -248,12 +265,180 @@ int launch_tc(const bf16* in, const bf16* w, const float* bias, const bf16* mask
     if (e != cudaSuccess) return lbm_set_err(nullptr, LBM_ECUDA, std::string("conv3d_tc_kernel: ") + cudaGetErrorString(e));
     return LBM_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Weight gradient on the tensor cores.  For one tap and one chunk of
+// WGT_CHUNK voxels, part[chunk][tap][co][ci] = sum_v g[v][co] * in[v + off][ci]
+// is a GEMM with M = co (TMEM lanes, rows >= cout stay zero), N = ci (TMEM
+// columns) and K = voxels.  g and in are channels-last, so each stage is
+// written into the K-major operand layout with a transposing store: a thread
+// loads 8 channels of one voxel (16 bytes) and stores them as 8 two-byte
+// elements of 8 operand rows.  The global loads of the next stage are issued
+// before the stores of the current one.  Partials are summed over chunks in a
+// fixed order by wgrad_reduce_kernel (nn_unet.cu).
+constexpr int WGT_CHUNK = 4096;
+constexpr int WGT_KV = 32;                 // voxels per stage (two K = 16 MMAs)
+constexpr int WGT_MAXA = 2, WGT_MAXB = 4;  // 16-byte loads per thread and stage (cout <= 64, cin <= 128)
+
+template <int CIN>
+__global__ void __launch_bounds__(TC_THREADS) conv3d_wgrad_tc_kernel(const bf16* __restrict__ in,
+                                                                    const bf16* __restrict__ g,
+                                                                    float* __restrict__ part, int N, int D, int H,
+                                                                    int W, int cout) {
+    constexpr uint32_t NCOL = CIN <= 32 ? 32 : (CIN <= 64 ? 64 : 128);
+    constexpr uint32_t IDESC = mma_idesc(TC_M, CIN);
+    constexpr uint32_t A_STEP = 4096u;                 // 128 rows x 32 B per K = 16
+    constexpr uint32_t B_STEP = (uint32_t)CIN * 32u;
+    constexpr uint32_t STAGE = 2 * (A_STEP + B_STEP);
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ uint64_t s_bar[3];
+    __shared__ uint32_t s_taddr;
+    __shared__ int s_fail;
+
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int tap = blockIdx.y;
+    const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+    const int64_t nvox = (int64_t)N * D * H * W;
+    const int64_t c0 = (int64_t)blockIdx.x * WGT_CHUNK;
+    const uint32_t smem0 = smem_u32(smem);
+
+    // zero both stages once: A rows >= cout are never written
+    for (uint32_t e = tid; e < 2 * STAGE / 16; e += TC_THREADS)
+        reinterpret_cast<uint4*>(smem)[e] = make_uint4(0u, 0u, 0u, 0u);
+    if (tid == 0) {
+        for (int b = 0; b < 3; ++b) mbar_init(&s_bar[b], 1);
+        s_fail = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&s_taddr)),
+                     "r"(NCOL)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t taddr = s_taddr;
+
+    const int ga = WGT_KV * (cout / 8), gb = WGT_KV * (CIN / 8);   // (voxel, 8-channel group) pairs
+    uint4 ra[WGT_MAXA], rb[WGT_MAXB];
+    auto fetch = [&](int q) {   // stage q's global data into registers
+        const int64_t s0 = c0 + (int64_t)q * WGT_KV;
+#pragma unroll
+        for (int u = 0; u < WGT_MAXA; ++u) {
+            const int e = tid + u * TC_THREADS;
+            uint4 val = make_uint4(0u, 0u, 0u, 0u);
+            if (e < ga) {
+                const int j = e % WGT_KV, c8 = e / WGT_KV;
+                const int64_t v = s0 + j;
+                if (v < nvox && v < c0 + WGT_CHUNK) val = *reinterpret_cast<const uint4*>(g + v * cout + c8 * 8);
+            }
+            ra[u] = val;
+        }
+#pragma unroll
+        for (int u = 0; u < WGT_MAXB; ++u) {
+            const int e = tid + u * TC_THREADS;
+            uint4 val = make_uint4(0u, 0u, 0u, 0u);
+            if (e < gb) {
+                const int j = e % WGT_KV, c8 = e / WGT_KV;
+                const int64_t v = s0 + j;
+                if (v < nvox && v < c0 + WGT_CHUNK) {
+                    int64_t t = v;
+                    const int x = (int)(t % W) + dx;
+                    t /= W;
+                    const int y = (int)(t % H) + dy;
+                    t /= H;
+                    const int z = (int)(t % D) + dz;
+                    const int nn = (int)(t / D);
+                    if (z >= 0 && z < D && y >= 0 && y < H && x >= 0 && x < W)
+                        val = *reinterpret_cast<const uint4*>(in + ((((int64_t)nn * D + z) * H + y) * W + x) * CIN + c8 * 8);
+                }
+            }
+            rb[u] = val;
+        }
+    };
+    // transposing store: element (row, k) of a K = 16 step at canon(row, k / 8) + (k % 8) * 2
+    auto put = [&](uint32_t base, uint32_t step_bytes, int j, int c8, const uint4& val) {
+        const uint32_t sub = base + (uint32_t)(j >> 4) * step_bytes;
+        const int k = j & 15;
+        const uint32_t off = (uint32_t)((k >> 3) * 128 + (k & 7) * 2);
+        const uint32_t w4[4] = {val.x, val.y, val.z, val.w};
+#pragma unroll
+        for (int h = 0; h < 8; ++h) {
+            const int row = c8 * 8 + h;
+            const uint16_t b16 = (uint16_t)(w4[h >> 1] >> ((h & 1) * 16));
+            const uint32_t addr = sub + (uint32_t)((row >> 3) * 256 + (row & 7) * 16) + off;
+            asm volatile("st.shared.u16 [%0], %1;" ::"r"(addr), "h"(b16) : "memory");
+        }
+    };
+
+    const int nq = WGT_CHUNK / WGT_KV;
+    fetch(0);
+#pragma unroll 1
+    for (int q = 0; q < nq; ++q) {
+        const int s = q & 1;
+        if (q >= 2) {   // the MMAs of step q - 2, which read stage s, have completed
+            if (!mbar_wait(&s_bar[s], (uint32_t)((q / 2 - 1) & 1))) s_fail = 1;
+            __syncthreads();
+            if (s_fail) break;
+        }
+        const uint32_t sa = smem0 + (uint32_t)s * STAGE, sb = sa + 2 * A_STEP;
+#pragma unroll
+        for (int u = 0; u < WGT_MAXA; ++u) {
+            const int e = tid + u * TC_THREADS;
+            if (e < ga) put(sa, A_STEP, e % WGT_KV, e / WGT_KV, ra[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < WGT_MAXB; ++u) {
+            const int e = tid + u * TC_THREADS;
+            if (e < gb) put(sb, B_STEP, e % WGT_KV, e / WGT_KV, rb[u]);
+        }
+        if (q + 1 < nq) fetch(q + 1);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+            for (int k2 = 0; k2 < 2; ++k2)
+                tc_mma(taddr, smem_desc(sa + k2 * A_STEP, 128, 256), smem_desc(sb + k2 * B_STEP, 128, 256), IDESC,
+                       (q > 0 || k2 > 0) ? 1u : 0u);
+            tc_commit(&s_bar[s]);
+        }
+    }
+    if (tid == 0) tc_commit(&s_bar[2]);
+    if (!mbar_wait(&s_bar[2], 0)) s_fail = 1;
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (!s_fail) {
+        if (warp * 32 < cout) {
+            const int co = warp * 32 + (tid & 31);
+            float* dst = part + (((int64_t)blockIdx.x * 27 + tap) * cout + co) * CIN;
+#pragma unroll
+            for (int c = 0; c < CIN; c += 16) {
+                float acc[16];
+                tc_ld16(taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, acc);
+                if (co < cout) {
+#pragma unroll
+                    for (int q4 = 0; q4 < 4; ++q4)
+                        reinterpret_cast<float4*>(dst + c)[q4] = make_float4(acc[4 * q4], acc[4 * q4 + 1], acc[4 * q4 + 2], acc[4 * q4 + 3]);
+                }
+            }
+        }
+    } else if (tid == 0) {
+        atomicExch(&g_tc_error, 1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(NCOL) : "memory");
+}
 }  // namespace
 
 extern "C" {
 
-int lbm_nn_conv3d_tc(const void* in, const void* w, const float* bias, const void* mask, void* out, int32_t n,
-                     int32_t d, int32_t h, int32_t wd, int32_t cin, int32_t cout, int32_t mode, void* stream) {
+int lbm_nn_conv3d(const void* in, const void* w, const float* bias, const void* mask, void* out, int32_t n, int32_t d,
+                  int32_t h, int32_t wd, int32_t cin, int32_t cout, int32_t mode, void* stream) {
     const int64_t nvox = (int64_t)n * d * h * wd;
     if (!in || !w || !out || nvox <= 0 || cin % 16 || cin <= 0 || cin > 128 || (mode != 0 && mode != 1))
         return lbm_set_err(nullptr, LBM_EINVAL, "lbm_nn_conv3d: cin must be a multiple of 16 in [16, 128]; mode 0 or 1");
@@ -286,3 +471,29 @@ int lbm_nn_tc_status(int32_t* timed_out) {
 }
 
 }  // extern "C"
+
+// Tensor-core weight-gradient partials (see conv3d_wgrad_tc_kernel); grid (chunks, 27).
+int nn_wgrad_tc_launch(const void* in, const void* g, float* part, int n, int d, int h, int w, int cin, int cout,
+                       cudaStream_t s) {
+    if (cin % 16 || cin < 16 || cin > 128 || cout % 8 || cout < 8 || cout > 64)
+        return lbm_set_err(nullptr, LBM_EINVAL, "lbm_nn_conv3d_wgrad: cin must be a multiple of 16 up to 128, cout a multiple of 8 up to 64");
+    const int64_t nvox = (int64_t)n * d * h * w;
+    const dim3 grid((unsigned)((nvox + WGT_CHUNK - 1) / WGT_CHUNK), 27);
+    const size_t smem = 2 * 2 * (4096 + (size_t)cin * 32);
+#define LBM_WG(C)                                                                                              \
+    case C: {                                                                                                  \
+        auto k = conv3d_wgrad_tc_kernel<C>;                                                                    \
+        if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)    \
+            return lbm_set_err(nullptr, LBM_ECUDA, "lbm_nn_conv3d_wgrad: shared memory attribute");            \
+        k<<<grid, TC_THREADS, smem, s>>>((const bf16*)in, (const bf16*)g, part, n, d, h, w, cout);             \
+        break;                                                                                                 \
+    }
+    switch (cin) {
+        LBM_WG(16) LBM_WG(32) LBM_WG(48) LBM_WG(64) LBM_WG(80) LBM_WG(96) LBM_WG(112) LBM_WG(128)
+    }
+#undef LBM_WG
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return lbm_set_err(nullptr, LBM_ECUDA, std::string("conv3d_wgrad_tc_kernel: ") + cudaGetErrorString(e));
+    return LBM_OK;
+}
+int64_t nn_wgrad_tc_chunks(int64_t nvox) { return (nvox + WGT_CHUNK - 1) / WGT_CHUNK; }

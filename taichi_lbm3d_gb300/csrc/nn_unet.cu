@@ -3,14 +3,9 @@
 // 1x1 output head, masked MSE, Adam.  Activations are BF16, channels last
 // (N, D, H, W, C); accumulation is FP32.
 //
-// conv3d_mma_kernel: implicit GEMM on the tensor cores (mma.sync m16n8k16
-// BF16 -> FP32).  M = voxels (16 per warp), N = output channels, K = 27 taps x
-// input channels; zero padding at the volume faces.  The same kernel computes
-// the backward-data pass with the tap-flipped, transposed weights.  Epilogues:
-// bias + ReLU (forward) or multiply by the ReLU mask of the layer input
-// (backward).  conv3d_wgrad_kernel: weight gradient on the CUDA cores (FP32
-// FMA, 4x4 register blocks), one partial per (voxel chunk, tap), summed in a
-// fixed order by a second kernel.
+// The 3x3x3 convolution (forward, backward data) and its weight gradient run
+// on the tcgen05 tensor cores (nn_tc.cu); the weight gradient leaves one FP32
+// partial per (voxel chunk, tap), summed here in a fixed order.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -20,20 +15,14 @@
 #include "../../include/lbm_nn.h"
 #include "lbm_internal.h"
 
+// tensor-core weight gradient (nn_tc.cu)
+int nn_wgrad_tc_launch(const void* in, const void* g, float* part, int n, int d, int h, int w, int cin, int cout,
+                       cudaStream_t s);
+int64_t nn_wgrad_tc_chunks(int64_t nvox);
+
 namespace {
 
 typedef __nv_bfloat16 bf16;
-
-__device__ __forceinline__ void mma_bf16(float* d, uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t b0,
-                                         uint32_t b1) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
-}
-
-__device__ __forceinline__ uint32_t ld32(const bf16* p) { return *reinterpret_cast<const uint32_t*>(p); }
 
 struct Vox {
     int n, z, y, x;
@@ -48,142 +37,6 @@ __device__ __forceinline__ Vox decode(int64_t v, int D, int H, int W) {
     o.z = (int)(t % D);
     o.n = (int)(t / D);
     return o;
-}
-
-// MODE 0: out = relu(acc + bias); MODE 1: out = acc * (mask > 0) (mask may be NULL).
-template <int NT, int MODE>
-__global__ void __launch_bounds__(128) conv3d_mma_kernel(const bf16* __restrict__ in, const bf16* __restrict__ w,
-                                                         const float* __restrict__ bias,
-                                                         const bf16* __restrict__ mask, bf16* __restrict__ out,
-                                                         int N, int D, int H, int W, int cin) {
-    constexpr int COUT = NT * 8;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int64_t nvox = (int64_t)N * D * H * W;
-    const int64_t v0 = ((int64_t)blockIdx.x * 4 + warp) * 16;
-    if (v0 >= nvox) return;
-    const int g = lane >> 2, q = lane & 3;
-    const int64_t va = v0 + g, vb = va + 8;
-    const Vox A = decode(va, D, H, W), B = decode(vb, D, H, W);
-    float acc[NT][4];
-#pragma unroll
-    for (int t = 0; t < NT; ++t) acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.f;
-    const int kc = cin >> 4;
-    for (int tap = 0; tap < 27; ++tap) {
-        const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
-        const int za = A.z + dz, ya = A.y + dy, xa = A.x + dx;
-        const int zb = B.z + dz, yb = B.y + dy, xb = B.x + dx;
-        const bool ina = za >= 0 && za < D && ya >= 0 && ya < H && xa >= 0 && xa < W;
-        const bool inb = zb >= 0 && zb < D && yb >= 0 && yb < H && xb >= 0 && xb < W;
-        const bf16* pa = in + ((((int64_t)A.n * D + za) * H + ya) * W + xa) * cin + q * 2;
-        const bf16* pb = in + ((((int64_t)B.n * D + zb) * H + yb) * W + xb) * cin + q * 2;
-        const bf16* wt = w + (int64_t)tap * cin + q * 2;
-        for (int c = 0; c < kc; ++c) {
-            const uint32_t a0 = ina ? ld32(pa + c * 16) : 0u;
-            const uint32_t a1 = inb ? ld32(pb + c * 16) : 0u;
-            const uint32_t a2 = ina ? ld32(pa + c * 16 + 8) : 0u;
-            const uint32_t a3 = inb ? ld32(pb + c * 16 + 8) : 0u;
-#pragma unroll
-            for (int t = 0; t < NT; ++t) {
-                const bf16* wp = wt + (int64_t)(t * 8 + g) * 27 * cin + c * 16;
-                mma_bf16(acc[t], a0, a1, a2, a3, ld32(wp), ld32(wp + 8));
-            }
-        }
-    }
-#pragma unroll
-    for (int t = 0; t < NT; ++t) {
-        const int co = t * 8 + q * 2;
-        float r0 = acc[t][0], r1 = acc[t][1], r2 = acc[t][2], r3 = acc[t][3];
-        if constexpr (MODE == 0) {
-            const float b0 = bias ? bias[co] : 0.f, b1 = bias ? bias[co + 1] : 0.f;
-            r0 = fmaxf(r0 + b0, 0.f);
-            r1 = fmaxf(r1 + b1, 0.f);
-            r2 = fmaxf(r2 + b0, 0.f);
-            r3 = fmaxf(r3 + b1, 0.f);
-        } else {
-            if (mask) {
-                const __nv_bfloat162 ma = *reinterpret_cast<const __nv_bfloat162*>(mask + va * COUT + co);
-                const __nv_bfloat162 mb = *reinterpret_cast<const __nv_bfloat162*>(mask + vb * COUT + co);
-                r0 = __bfloat162float(ma.x) > 0.f ? r0 : 0.f;
-                r1 = __bfloat162float(ma.y) > 0.f ? r1 : 0.f;
-                r2 = __bfloat162float(mb.x) > 0.f ? r2 : 0.f;
-                r3 = __bfloat162float(mb.y) > 0.f ? r3 : 0.f;
-            }
-        }
-        *reinterpret_cast<__nv_bfloat162*>(out + va * COUT + co) = __floats2bfloat162_rn(r0, r1);
-        *reinterpret_cast<__nv_bfloat162*>(out + vb * COUT + co) = __floats2bfloat162_rn(r2, r3);
-    }
-}
-
-// Weight gradient partials: part[chunk][tap][co][ci] = sum over the chunk's
-// voxels v of g[v][co] * in[v + off(tap)][ci].
-constexpr int WG_CHUNK = 4096, WG_SUB = 32;
-__global__ void __launch_bounds__(256) conv3d_wgrad_kernel(const bf16* __restrict__ in, const bf16* __restrict__ g,
-                                                           float* __restrict__ part, int N, int D, int H, int W,
-                                                           int cin, int cout) {
-    extern __shared__ float sm[];
-    float* sg = sm;                       // [WG_SUB][cout]
-    float* si = sm + WG_SUB * cout;       // [WG_SUB][cin]
-    const int tap = blockIdx.y;
-    const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
-    const int64_t nvox = (int64_t)N * D * H * W;
-    const int64_t c0 = (int64_t)blockIdx.x * WG_CHUNK;
-    const int nco = cout / 4, nci = cin / 4;   // 4x4 blocks
-    const int nblk = nco * nci;
-    float acc[2][16];
-#pragma unroll
-    for (int r = 0; r < 2; ++r)
-#pragma unroll
-        for (int e = 0; e < 16; ++e) acc[r][e] = 0.f;
-    for (int64_t s0 = c0; s0 < c0 + WG_CHUNK && s0 < nvox; s0 += WG_SUB) {
-        for (int e = threadIdx.x; e < WG_SUB * cout; e += blockDim.x) {
-            const int64_t v = s0 + e / cout;
-            sg[e] = v < nvox ? __bfloat162float(g[v * cout + e % cout]) : 0.f;
-        }
-        for (int e = threadIdx.x; e < WG_SUB * cin; e += blockDim.x) {
-            const int64_t v = s0 + e / cin;
-            float val = 0.f;
-            if (v < nvox) {
-                const Vox P = decode(v, D, H, W);
-                const int z = P.z + dz, y = P.y + dy, x = P.x + dx;
-                if (z >= 0 && z < D && y >= 0 && y < H && x >= 0 && x < W)
-                    val = __bfloat162float(in[((((int64_t)P.n * D + z) * H + y) * W + x) * cin + e % cin]);
-            }
-            si[e] = val;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int r = 0; r < 2; ++r) {
-            const int b = threadIdx.x + r * blockDim.x;
-            if (b < nblk) {
-                const int bo = (b / nci) * 4, bi = (b % nci) * 4;
-                for (int vv = 0; vv < WG_SUB; ++vv) {
-                    float gg[4], ii[4];
-#pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        gg[u] = sg[vv * cout + bo + u];
-                        ii[u] = si[vv * cin + bi + u];
-                    }
-#pragma unroll
-                    for (int u = 0; u < 4; ++u)
-#pragma unroll
-                        for (int l = 0; l < 4; ++l) acc[r][u * 4 + l] = fmaf(gg[u], ii[l], acc[r][u * 4 + l]);
-                }
-            }
-        }
-        __syncthreads();
-    }
-    float* dst = part + ((int64_t)blockIdx.x * 27 + tap) * cout * cin;
-#pragma unroll
-    for (int r = 0; r < 2; ++r) {
-        const int b = threadIdx.x + r * blockDim.x;
-        if (b < nblk) {
-            const int bo = (b / nci) * 4, bi = (b % nci) * 4;
-#pragma unroll
-            for (int u = 0; u < 4; ++u)
-#pragma unroll
-                for (int l = 0; l < 4; ++l) dst[(bo + u) * cin + bi + l] = acc[r][u * 4 + l];
-        }
-    }
 }
 
 // dw[co][tap][ci] = sum over chunks (fixed order) of part[chunk][tap][co][ci].
@@ -424,49 +277,19 @@ int check(const char* what) {
 
 extern "C" {
 
-int lbm_nn_conv3d(const void* in, const void* w, const float* bias, const void* mask, void* out, int32_t n, int32_t d,
-                  int32_t h, int32_t wd, int32_t cin, int32_t cout, int32_t mode, void* stream) {
-    const int64_t nvox = (int64_t)n * d * h * wd;
-    if (!in || !w || !out || nvox <= 0 || nvox % 16 || cin % 16 || cin <= 0 || (mode != 0 && mode != 1))
-        return lbm_set_err(nullptr, LBM_EINVAL, "lbm_nn_conv3d: voxels and cin must be multiples of 16; mode 0 or 1");
-    cudaStream_t s = (cudaStream_t)stream;
-    const int grid = (int)((nvox / 16 + 3) / 4);
-    const bf16* I = (const bf16*)in;
-    const bf16* Wt = (const bf16*)w;
-    const bf16* M = (const bf16*)mask;
-    bf16* O = (bf16*)out;
-#define LBM_CONV(NT)                                                                                  \
-    case NT * 8:                                                                                      \
-        if (mode == 0) conv3d_mma_kernel<NT, 0><<<grid, 128, 0, s>>>(I, Wt, bias, M, O, n, d, h, wd, cin); \
-        else conv3d_mma_kernel<NT, 1><<<grid, 128, 0, s>>>(I, Wt, bias, M, O, n, d, h, wd, cin);          \
-        break;
-    switch (cout) {
-        LBM_CONV(2) LBM_CONV(4) LBM_CONV(6) LBM_CONV(8) LBM_CONV(12)
-    default:
-        return lbm_set_err(nullptr, LBM_EINVAL, "lbm_nn_conv3d: cout must be 16, 32, 48, 64 or 96");
-    }
-#undef LBM_CONV
-    return check("conv3d_mma_kernel");
-}
-
 int64_t lbm_nn_wgrad_scratch_floats(int32_t n, int32_t d, int32_t h, int32_t w, int32_t cin, int32_t cout) {
-    const int64_t nvox = (int64_t)n * d * h * w;
-    return ((nvox + WG_CHUNK - 1) / WG_CHUNK) * 27 * (int64_t)cin * cout;
+    return nn_wgrad_tc_chunks((int64_t)n * d * h * w) * 27 * (int64_t)cin * cout;
 }
 
 int lbm_nn_conv3d_wgrad(const void* in, const void* g, float* dw, float* db, float* scratch, int64_t scratch_floats,
                         int32_t n, int32_t d, int32_t h, int32_t w, int32_t cin, int32_t cout, void* stream) {
     const int64_t nvox = (int64_t)n * d * h * w;
-    if (!in || !g || !dw || !scratch || cin % 4 || cout % 4 || (cin / 4) * (cout / 4) > 512)
-        return lbm_set_err(nullptr, LBM_EINVAL, "lbm_nn_conv3d_wgrad: bad arguments");
+    if (!in || !g || !dw || !scratch || nvox <= 0) return lbm_set_err(nullptr, LBM_EINVAL, "lbm_nn_conv3d_wgrad: bad arguments");
     if (scratch_floats < lbm_nn_wgrad_scratch_floats(n, d, h, w, cin, cout))
         return lbm_set_err(nullptr, LBM_EINVAL, "lbm_nn_conv3d_wgrad: scratch too small");
     cudaStream_t s = (cudaStream_t)stream;
-    const int nchunk = (int)((nvox + WG_CHUNK - 1) / WG_CHUNK);
-    const size_t smem = sizeof(float) * WG_SUB * (cin + cout);
-    conv3d_wgrad_kernel<<<dim3(nchunk, 27), 256, smem, s>>>((const bf16*)in, (const bf16*)g, scratch, n, d, h, w, cin,
-                                                          cout);
-    int rc = check("conv3d_wgrad_kernel");
+    const int nchunk = (int)nn_wgrad_tc_chunks(nvox);
+    int rc = nn_wgrad_tc_launch(in, g, scratch, n, d, h, w, cin, cout, s);
     if (rc) return rc;
     wgrad_reduce_kernel<<<blocks((int64_t)27 * cin * cout), 256, 0, s>>>(scratch, dw, nchunk, cin, cout);
     rc = check("wgrad_reduce_kernel");

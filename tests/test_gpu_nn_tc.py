@@ -1,6 +1,6 @@
-"""Tensor-core (tcgen05) 3x3x3 convolution against an FP64 numpy reference
-and against the mma.sync kernel, for the channel counts of the network, both
-modes, and voxel counts that leave a partial 128-voxel tile."""
+"""Tensor-core (tcgen05) 3x3x3 convolution against an FP64 numpy reference,
+for the channel counts of the network, both modes, and a voxel count that
+leaves a partial 128-voxel tile; the pipeline's timeout flag stays clear."""
 import ctypes
 
 import numpy as np
@@ -36,7 +36,7 @@ def test_tc_conv_matches_reference(cin, cout, mode):
     out_tc = torch.zeros((1, D, H, W, cout), dtype=torch.bfloat16, device="cuda")
     s = torch.cuda.current_stream().cuda_stream
     p = lambda t: ctypes.c_void_p(t.data_ptr())
-    rc = L.lbm_nn_conv3d_tc(p(xg), p(wg), p(bg) if mode == 0 else None, p(mg) if mode == 1 else None, p(out_tc),
+    rc = L.lbm_nn_conv3d(p(xg), p(wg), p(bg) if mode == 0 else None, p(mg) if mode == 1 else None, p(out_tc),
                             1, D, H, W, cin, cout, mode, ctypes.c_void_p(s))
     assert rc == 0
     torch.cuda.synchronize()
@@ -47,3 +47,34 @@ def test_tc_conv_matches_reference(cin, cout, mode):
                  b.numpy().astype(np.float64) if mode == 0 else None, m.float().numpy()[0], mode)
     err = np.abs(y - r).max() / max(np.abs(r).max(), 1e-30)
     assert err < 1e-2, err
+
+
+@pytest.mark.parametrize("cin,cout", [(16, 16), (16, 32), (32, 64), (64, 64), (96, 32), (48, 16), (32, 32)])
+def test_tc_weight_gradient_matches_reference(cin, cout):
+    """dw[co][tap][ci] = sum_v g[v][co] x[v + off(tap)][ci] and db = sum_v g,
+    against FP64 on a volume whose voxel count is not a multiple of the
+    4096-voxel chunk."""
+    import torch
+    from oracle.unet_oracle import conv_bwd
+    from taichi_lbm3d_gb300 import unet
+    L = unet._lib()
+    rng = np.random.default_rng(cin * 7 + cout)
+    D, H, W = 9, 23, 25                      # 5175 voxels: one full chunk and a partial one
+    x = torch.from_numpy(rng.standard_normal((1, D, H, W, cin)).astype(np.float32)).to(torch.bfloat16)
+    g = torch.from_numpy(rng.standard_normal((1, D, H, W, cout)).astype(np.float32)).to(torch.bfloat16)
+    xg, gg = x.cuda().contiguous(), g.cuda().contiguous()
+    dw = torch.zeros((cout, 27, cin), device="cuda")
+    db = torch.zeros(cout, device="cuda")
+    nscr = L.lbm_nn_wgrad_scratch_floats(1, D, H, W, cin, cout)
+    scr = torch.empty(int(nscr), device="cuda")
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert L.lbm_nn_conv3d_wgrad(p(xg), p(gg), p(dw), p(db), p(scr), scr.numel(), 1, D, H, W, cin, cout, s) == 0
+    torch.cuda.synchronize()
+    flag = ctypes.c_int32(7)
+    assert L.lbm_nn_tc_status(ctypes.byref(flag)) == 0 and flag.value == 0
+    _, dw_ref, db_ref = conv_bwd(x.float().numpy()[0].astype(np.float64), np.zeros((cout, 27, cin)),
+                                 g.float().numpy()[0].astype(np.float64))
+    e_w = np.abs(dw.cpu().numpy() - dw_ref).max() / np.abs(dw_ref).max()
+    e_b = np.abs(db.cpu().numpy() - db_ref).max() / np.abs(db_ref).max()
+    assert e_w < 1e-4 and e_b < 1e-4, (e_w, e_b)
