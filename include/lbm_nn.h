@@ -31,7 +31,9 @@ int lbm_nn_tc_status(int32_t* timed_out);
 /* wt[ci][tap][co] = w[co][26 - tap][ci]: weights of the backward-data conv. */
 int lbm_nn_flip_transpose(const void* w, void* wt, int32_t cin, int32_t cout, void* stream);
 /* Weight gradient dw[co][tap][ci] (FP32) and bias gradient db[co] (may be NULL)
- * of the conv with input `in` and output gradient `g`; scratch of
+ * of the conv with input `in` and output gradient `g`, on the tcgen05 tensor
+ * cores (per-chunk FP32 partials summed in a fixed order); cin a multiple of
+ * 16 up to 128, cout a multiple of 8 up to 64; scratch of
  * lbm_nn_wgrad_scratch_floats() floats. */
 int64_t lbm_nn_wgrad_scratch_floats(int32_t n, int32_t d, int32_t h, int32_t w, int32_t cin, int32_t cout);
 int lbm_nn_conv3d_wgrad(const void* in, const void* g, float* dw, float* db, float* scratch, int64_t scratch_floats,

@@ -275,25 +275,30 @@ int launch_tc(const bf16* in, const bf16* w, const float* bias, const bf16* mask
 // loads 8 channels of one voxel (16 bytes) and stores them as 8 two-byte
 // elements of 8 operand rows.  The global loads of the next stage are issued
 // before the stores of the current one.  Partials are summed over chunks in a
-// fixed order by wgrad_reduce_kernel (nn_unet.cu).
+// fixed order by wgrad_reduce_kernel (nn_unet.cu).  The CTAs of the centre
+// tap (no shift) also sum g over their chunk from the same loads: the bias
+// gradient partials dbpart[chunk][co].
 constexpr int WGT_CHUNK = 4096;
-constexpr int WGT_KV = 32;                 // voxels per stage (two K = 16 MMAs)
-constexpr int WGT_MAXA = 2, WGT_MAXB = 4;  // 16-byte loads per thread and stage (cout <= 64, cin <= 128)
+constexpr int WGT_KV = 64;                 // voxels per stage (four K = 16 MMAs)
+constexpr int WGT_MAXA = 4, WGT_MAXB = 8;  // 16-byte loads per thread and stage (cout <= 64, cin <= 128)
 
 template <int CIN>
 __global__ void __launch_bounds__(TC_THREADS) conv3d_wgrad_tc_kernel(const bf16* __restrict__ in,
                                                                     const bf16* __restrict__ g,
-                                                                    float* __restrict__ part, int N, int D, int H,
+                                                                    float* __restrict__ part,
+                                                                    float* __restrict__ dbpart, int N, int D, int H,
                                                                     int W, int cout) {
     constexpr uint32_t NCOL = CIN <= 32 ? 32 : (CIN <= 64 ? 64 : 128);
     constexpr uint32_t IDESC = mma_idesc(TC_M, CIN);
     constexpr uint32_t A_STEP = 4096u;                 // 128 rows x 32 B per K = 16
     constexpr uint32_t B_STEP = (uint32_t)CIN * 32u;
-    constexpr uint32_t STAGE = 2 * (A_STEP + B_STEP);
+    constexpr int KS = WGT_KV / 16;                    // MMAs per stage
+    constexpr uint32_t STAGE = KS * (A_STEP + B_STEP);
     extern __shared__ __align__(1024) unsigned char smem[];
     __shared__ uint64_t s_bar[3];
     __shared__ uint32_t s_taddr;
     __shared__ int s_fail;
+    __shared__ float s_db[64];
 
     const int tid = threadIdx.x, warp = tid >> 5;
     const int tap = blockIdx.y;
@@ -310,6 +315,7 @@ __global__ void __launch_bounds__(TC_THREADS) conv3d_wgrad_tc_kernel(const bf16*
         s_fail = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
+    if (tid < 64) s_db[tid] = 0.f;
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&s_taddr)),
                      "r"(NCOL)
@@ -320,6 +326,12 @@ __global__ void __launch_bounds__(TC_THREADS) conv3d_wgrad_tc_kernel(const bf16*
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t taddr = s_taddr;
+    const bool centre = tap == 13;
+    float dbacc[WGT_MAXA][8];
+#pragma unroll
+    for (int u = 0; u < WGT_MAXA; ++u)
+#pragma unroll
+        for (int h = 0; h < 8; ++h) dbacc[u][h] = 0.f;
 
     const int ga = WGT_KV * (cout / 8), gb = WGT_KV * (CIN / 8);   // (voxel, 8-channel group) pairs
     uint4 ra[WGT_MAXA], rb[WGT_MAXB];
@@ -383,11 +395,19 @@ __global__ void __launch_bounds__(TC_THREADS) conv3d_wgrad_tc_kernel(const bf16*
             __syncthreads();
             if (s_fail) break;
         }
-        const uint32_t sa = smem0 + (uint32_t)s * STAGE, sb = sa + 2 * A_STEP;
+        const uint32_t sa = smem0 + (uint32_t)s * STAGE, sb = sa + KS * A_STEP;
 #pragma unroll
         for (int u = 0; u < WGT_MAXA; ++u) {
             const int e = tid + u * TC_THREADS;
-            if (e < ga) put(sa, A_STEP, e % WGT_KV, e / WGT_KV, ra[u]);
+            if (e < ga) {
+                put(sa, A_STEP, e % WGT_KV, e / WGT_KV, ra[u]);
+                if (centre) {
+                    const uint32_t w4[4] = {ra[u].x, ra[u].y, ra[u].z, ra[u].w};
+#pragma unroll
+                    for (int h = 0; h < 8; ++h)
+                        dbacc[u][h] += __uint_as_float((w4[h >> 1] >> ((h & 1) * 16)) << 16);
+                }
+            }
         }
 #pragma unroll
         for (int u = 0; u < WGT_MAXB; ++u) {
@@ -400,13 +420,26 @@ __global__ void __launch_bounds__(TC_THREADS) conv3d_wgrad_tc_kernel(const bf16*
         if (tid == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
-            for (int k2 = 0; k2 < 2; ++k2)
+            for (int k2 = 0; k2 < KS; ++k2)
                 tc_mma(taddr, smem_desc(sa + k2 * A_STEP, 128, 256), smem_desc(sb + k2 * B_STEP, 128, 256), IDESC,
                        (q > 0 || k2 > 0) ? 1u : 0u);
             tc_commit(&s_bar[s]);
         }
     }
     if (tid == 0) tc_commit(&s_bar[2]);
+    if (centre) {   // bias-gradient partial of this chunk: fixed-order shared reduction
+        for (int j0 = 0; j0 < WGT_KV; ++j0) {
+#pragma unroll
+            for (int u = 0; u < WGT_MAXA; ++u) {
+                const int e = tid + u * TC_THREADS;
+                if (e < ga && e % WGT_KV == j0)
+#pragma unroll
+                    for (int h = 0; h < 8; ++h) s_db[(e / WGT_KV) * 8 + h] += dbacc[u][h];
+            }
+            __syncthreads();
+        }
+        if (tid < cout) dbpart[(int64_t)blockIdx.x * cout + tid] = s_db[tid];
+    }
     if (!mbar_wait(&s_bar[2], 0)) s_fail = 1;
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -473,19 +506,19 @@ int lbm_nn_tc_status(int32_t* timed_out) {
 }  // extern "C"
 
 // Tensor-core weight-gradient partials (see conv3d_wgrad_tc_kernel); grid (chunks, 27).
-int nn_wgrad_tc_launch(const void* in, const void* g, float* part, int n, int d, int h, int w, int cin, int cout,
-                       cudaStream_t s) {
+int nn_wgrad_tc_launch(const void* in, const void* g, float* part, float* dbpart, int n, int d, int h, int w, int cin,
+                       int cout, cudaStream_t s) {
     if (cin % 16 || cin < 16 || cin > 128 || cout % 8 || cout < 8 || cout > 64)
         return lbm_set_err(nullptr, LBM_EINVAL, "lbm_nn_conv3d_wgrad: cin must be a multiple of 16 up to 128, cout a multiple of 8 up to 64");
     const int64_t nvox = (int64_t)n * d * h * w;
     const dim3 grid((unsigned)((nvox + WGT_CHUNK - 1) / WGT_CHUNK), 27);
-    const size_t smem = 2 * 2 * (4096 + (size_t)cin * 32);
+    const size_t smem = 2 * (WGT_KV / 16) * (4096 + (size_t)cin * 32);
 #define LBM_WG(C)                                                                                              \
     case C: {                                                                                                  \
         auto k = conv3d_wgrad_tc_kernel<C>;                                                                    \
         if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)    \
             return lbm_set_err(nullptr, LBM_ECUDA, "lbm_nn_conv3d_wgrad: shared memory attribute");            \
-        k<<<grid, TC_THREADS, smem, s>>>((const bf16*)in, (const bf16*)g, part, n, d, h, w, cout);             \
+        k<<<grid, TC_THREADS, smem, s>>>((const bf16*)in, (const bf16*)g, part, dbpart, n, d, h, w, cout);     \
         break;                                                                                                 \
     }
     switch (cin) {

@@ -16,8 +16,8 @@
 #include "lbm_internal.h"
 
 // tensor-core weight gradient (nn_tc.cu)
-int nn_wgrad_tc_launch(const void* in, const void* g, float* part, int n, int d, int h, int w, int cin, int cout,
-                       cudaStream_t s);
+int nn_wgrad_tc_launch(const void* in, const void* g, float* part, float* dbpart, int n, int d, int h, int w, int cin,
+                       int cout, cudaStream_t s);
 int64_t nn_wgrad_tc_chunks(int64_t nvox);
 
 namespace {
@@ -52,20 +52,13 @@ __global__ void wgrad_reduce_kernel(const float* __restrict__ part, float* __res
     dw[((int64_t)co * 27 + tap) * cin + ci] = s;
 }
 
-// db[co] = sum over voxels of g[v][co] (one block per channel, fixed order tree).
-__global__ void __launch_bounds__(256) bias_grad_kernel(const bf16* __restrict__ g, float* __restrict__ db,
-                                                        int64_t nvox, int cout) {
-    __shared__ float sh[256];
-    const int co = blockIdx.x;
+// db[co] = sum over chunks (fixed order) of dbpart[chunk][co].
+__global__ void bias_reduce_kernel(const float* __restrict__ dbpart, float* __restrict__ db, int nchunk, int cout) {
+    const int co = blockIdx.x * blockDim.x + threadIdx.x;
+    if (co >= cout) return;
     float s = 0.f;
-    for (int64_t v = threadIdx.x; v < nvox; v += 256) s += __bfloat162float(g[v * cout + co]);
-    sh[threadIdx.x] = s;
-    __syncthreads();
-    for (int o = 128; o > 0; o >>= 1) {
-        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) db[co] = sh[0];
+    for (int c = 0; c < nchunk; ++c) s += dbpart[(int64_t)c * cout + co];
+    db[co] = s;
 }
 
 // wt[ci][tap][co] = w[co][26 - tap][ci]
@@ -278,7 +271,7 @@ int check(const char* what) {
 extern "C" {
 
 int64_t lbm_nn_wgrad_scratch_floats(int32_t n, int32_t d, int32_t h, int32_t w, int32_t cin, int32_t cout) {
-    return nn_wgrad_tc_chunks((int64_t)n * d * h * w) * 27 * (int64_t)cin * cout;
+    return nn_wgrad_tc_chunks((int64_t)n * d * h * w) * (27 * (int64_t)cin * cout + cout);
 }
 
 int lbm_nn_conv3d_wgrad(const void* in, const void* g, float* dw, float* db, float* scratch, int64_t scratch_floats,
@@ -289,13 +282,14 @@ int lbm_nn_conv3d_wgrad(const void* in, const void* g, float* dw, float* db, flo
         return lbm_set_err(nullptr, LBM_EINVAL, "lbm_nn_conv3d_wgrad: scratch too small");
     cudaStream_t s = (cudaStream_t)stream;
     const int nchunk = (int)nn_wgrad_tc_chunks(nvox);
-    int rc = nn_wgrad_tc_launch(in, g, scratch, n, d, h, w, cin, cout, s);
+    float* dbpart = scratch + (int64_t)nchunk * 27 * cin * cout;
+    int rc = nn_wgrad_tc_launch(in, g, scratch, dbpart, n, d, h, w, cin, cout, s);
     if (rc) return rc;
     wgrad_reduce_kernel<<<blocks((int64_t)27 * cin * cout), 256, 0, s>>>(scratch, dw, nchunk, cin, cout);
     rc = check("wgrad_reduce_kernel");
     if (rc || !db) return rc;
-    bias_grad_kernel<<<cout, 256, 0, s>>>((const bf16*)g, db, nvox, cout);
-    return check("bias_grad_kernel");
+    bias_reduce_kernel<<<blocks(cout), 256, 0, s>>>(dbpart, db, nchunk, cout);
+    return check("bias_reduce_kernel");
 }
 
 int lbm_nn_flip_transpose(const void* w, void* wt, int32_t cin, int32_t cout, void* stream) {
