@@ -334,6 +334,7 @@ def two_phase(steps=20000, every=500, shape=(131, 131, 131), storages=("f64", "f
         s.init_simulation()
         return s
 
+    every = min(every, steps)
     out = {"n_fluid": int((solid == 0).sum()), "steps": steps, "every": every}
     curves = {}
     for sto in storages:
@@ -350,7 +351,7 @@ def two_phase(steps=20000, every=500, shape=(131, 131, 131), storages=("f64", "f
         if sto != "f64":
             s = make(sto)
             lat = s._lat
-            nsteps = 2000
+            nsteps = min(2000, steps)
             stream = torch.cuda.ExternalStream(lat.stream())
             lat.step_async(20)
             lat.synchronize()
@@ -375,6 +376,45 @@ def two_phase(steps=20000, every=500, shape=(131, 131, 131), storages=("f64", "f
     return out
 
 
+def unet_step(steps=10, warmup=3, n=2, edge=96):
+    """Warm-start U-Net training step (forward, masked MSE, backward, Adam) on
+    n seeded random samples of edge^3 with 16 input channels: ms per step from
+    CUDA events, and the convolution work per step (forward, backward-data and
+    weight gradient: 3 x 2 x voxels x 27 x cin x cout per layer) in TFLOP/s."""
+    import torch
+    from taichi_lbm3d_gb300.unet import LAYERS, UNet3D
+    torch.manual_seed(0)
+    m = UNet3D(seed=0)
+    x = torch.randn((n, edge, edge, edge, 16), device="cuda").to(torch.bfloat16)
+    t = torch.randn((n, edge, edge, edge, 4), device="cuda")
+    mk = torch.ones((n, edge, edge, edge), device="cuda", dtype=torch.uint8)
+
+    def one():
+        y = m.forward(x)
+        loss, gy = m.loss(y, t, mk, float(mk.numel()) * 4)
+        m.backward(gy)
+        m.adam_step(lr=1e-4)
+        return loss
+
+    for _ in range(warmup):
+        one()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        loss = one()
+    e1.record()
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    flop = 0.0
+    for _, cin, cout, lv in LAYERS:
+        vox = n * (edge >> lv) ** 3
+        flop += 3 * 2.0 * vox * 27 * cin * cout
+    return {"workload": "U-Net training step, %d x %d^3, 16 input channels, random data" % (n, edge),
+            "steps": steps, "ms_per_step": ms, "conv_tflops": flop / (ms * 1e-3) / 1e12,
+            "loss_finite": bool(torch.isfinite(loss).all().item())}
+
+
 def grey_field(shape=SHAPE):
     """Grey-scale workload: the 256^3 pack of the default bench with ns = 1 in
     the spheres and a grey layer ns = 0.25 on pore cells within 1.5 cells of a
@@ -389,7 +429,7 @@ def grey_field(shape=SHAPE):
     return ns
 
 
-def grey(steps=1000, cpu_seconds=20.0, log=lambda m: print(m, file=sys.stderr, flush=True)):
+def grey(steps=1000, cpu=True, cpu_seconds=20.0, log=lambda m: print(m, file=sys.stderr, flush=True)):
     """Grey-scale (partial bounce-back) step on the grey 256^3 field: body
     force fx = 1e-6, periodic, niu 0.1 (script conventions).  MLUPS with CUDA
     events on the library's stream, FP32 and FP16; the CPU oracle's grey sweeps
@@ -429,6 +469,10 @@ def grey(steps=1000, cpu_seconds=20.0, log=lambda m: print(m, file=sys.stderr, f
         log("grey %s: %.0f MLUPS (%.0f GB/s algorithmic, %.1f%% of %s HBM copy)" % (
             sto, mlups, bpn * mlups / 1e3, 100 * bpn * mlups / 1e3 / peak, kind))
         lb.close()
+    out["peak_gbs"] = peak
+    out["peak_kind"] = kind
+    if not cpu:
+        return out
     from oracle.oracle import Oracle, make_params
     p = make_params(SHAPE, niu=0.1, force=(1e-6, 0, 0), visc_convention=1, guo_convention=1, bc_form=1, grey=True)
     o = Oracle(p, (ns.astype(int) != 0).astype(np.int8))
@@ -443,8 +487,6 @@ def grey(steps=1000, cpu_seconds=20.0, log=lambda m: print(m, file=sys.stderr, f
     o.close()
     out["cpu_baseline"] = {"value": nf * n / t / 1e6, "unit": UNIT, "cores": len(os.sched_getaffinity(0)),
                            "kind": "port", "sample": "%d grey steps of the full 256^3 lattice (%.1f s)" % (n, t)}
-    out["peak_gbs"] = peak
-    out["peak_kind"] = kind
     return out
 
 
@@ -482,7 +524,8 @@ def voxelize_bench(log=lambda m: print(m, file=sys.stderr, flush=True)):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default 2000; the --grey/--two-phase/--unet modes have their own defaults)")
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -495,16 +538,22 @@ def main():
     ap.add_argument("--two-phase", action="store_true", help="config 3: two-phase drainage vs FP64")
     ap.add_argument("--grey", action="store_true", help="grey-scale (partial bounce-back) step on a 256^3 grey field")
     ap.add_argument("--voxelize", action="store_true", help="STL voxeliser on a NACA wing in the reference box")
+    ap.add_argument("--unet", action="store_true", help="warm-start U-Net training step on 2 x 96^3")
     a = ap.parse_args()
     if a.voxelize:
         print(json.dumps({"voxelize": voxelize_bench()}))
         return 0
+    if a.unet:
+        print(json.dumps({"unet": unet_step(steps=a.steps or 10)}))
+        return 0
     if a.grey:
-        print(json.dumps({"grey": grey()}))
+        print(json.dumps({"grey": grey(steps=a.steps or 1000, cpu=not a.no_cpu_baseline)}))
         return 0
     if a.two_phase:
-        print(json.dumps({"two_phase": two_phase()}))
+        print(json.dumps({"two_phase": two_phase(steps=a.steps or 20000)}))
         return 0
+    if a.steps is None:
+        a.steps = 2000
     if a.batched:
         res = batched(n_sub=a.n_sub)
         print(json.dumps({"batched": res}))
