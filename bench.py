@@ -376,6 +376,48 @@ def two_phase(steps=20000, every=500, shape=(131, 131, 131), storages=("f64", "f
     return out
 
 
+def cavity(steps=1000, log=lambda m: print(m, file=sys.stderr, flush=True)):
+    """Config 1: 64^3 lid-driven cavity (one-node solid shell on five faces,
+    top z face fixed velocity (0.1, 0, 0), niu 0.1, FP32 reference
+    arithmetic, class conventions): GPU MLUPS over `steps` steps with CUDA
+    events, the CPU oracle over the same steps on all host cores, and the
+    largest rho/v difference between the two after `steps` steps."""
+    import torch
+    from oracle.oracle import Oracle, make_params as oracle_params
+    from taichi_lbm3d_gb300 import _native
+    from taichi_lbm3d_gb300.geometry import cavity_shell
+    solid = cavity_shell(64)
+    vel = [[0.0, 0.0, 0.0]] * 5 + [[0.1, 0.0, 0.0]]
+    op = oracle_params((64, 64, 64), niu=0.1, bc=(0, 0, 0, 0, 0, 2), vel_bc=vel)
+    p = _native.make_params((64, 64, 64), niu=0.1, bc=(0, 0, 0, 0, 0, 2), vel_bc=vel)
+    lat = _native.Lattice(p)
+    lat.set_geometry(solid)
+    lat.init()
+    nf = lat.info().n_fluid
+    stream = torch.cuda.ExternalStream(lat.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    lat.step_async(steps)
+    e1.record(stream)
+    e1.synchronize()
+    gpu_s = e0.elapsed_time(e1) / 1e3
+    rho, v = lat.macros()
+    o = Oracle(op, solid)
+    t = time.perf_counter()
+    o.step(steps)
+    cpu_s = time.perf_counter() - t
+    fl = solid == 0
+    d_rho = float(np.abs(rho[fl] - o.field("rho").astype(np.float32)[fl]).max())
+    d_v = float(np.abs(v[fl] - o.field("v").astype(np.float32)[fl]).max())
+    log("cavity: GPU %.0f MLUPS, CPU oracle %.1f MLUPS, max |drho| %g |dv| %g" % (
+        nf * steps / gpu_s / 1e6, nf * steps / cpu_s / 1e6, d_rho, d_v))
+    return {"workload": "64^3 lid-driven cavity, top face v = (0.1, 0, 0), niu 0.1, FP32, %d steps from rest" % steps,
+            "n_fluid": nf, "gpu_mlups": nf * steps / gpu_s / 1e6, "gpu_seconds": gpu_s,
+            "cpu_oracle_mlups": nf * steps / cpu_s / 1e6, "cpu_cores": len(os.sched_getaffinity(0)),
+            "max_abs_diff_rho_vs_oracle": d_rho, "max_abs_diff_v_vs_oracle": d_v,
+            "note": "first launches included (no warm-up): the lattice is L2-resident"}
+
+
 def unet_step(steps=10, warmup=3, n=2, edge=96):
     """Warm-start U-Net training step (forward, masked MSE, backward, Adam) on
     n seeded random samples of edge^3 with 16 input channels: ms per step from
@@ -539,7 +581,11 @@ def main():
     ap.add_argument("--grey", action="store_true", help="grey-scale (partial bounce-back) step on a 256^3 grey field")
     ap.add_argument("--voxelize", action="store_true", help="STL voxeliser on a NACA wing in the reference box")
     ap.add_argument("--unet", action="store_true", help="warm-start U-Net training step on 2 x 96^3")
+    ap.add_argument("--cavity", action="store_true", help="config 1: 64^3 lid-driven cavity, GPU vs CPU oracle")
     a = ap.parse_args()
+    if a.cavity:
+        print(json.dumps({"cavity": cavity(steps=a.steps or 1000)}))
+        return 0
     if a.voxelize:
         print(json.dumps({"voxelize": voxelize_bench()}))
         return 0

@@ -160,20 +160,33 @@ __global__ void __launch_bounds__(TC_THREADS) conv3d_tc_kernel(const bf16* __res
     // gather K step q (tap q / kc, channels 16 (q % kc) .. +15) into stage s:
     // A = this thread's shifted input row (zero outside the volume),
     // B = w[co][tap][ci] (row co, K = ci).  cp.async.ca keeps the input rows in
-    // L1, where the 27 taps of neighbouring voxels find them again.
+    // L1, where the 27 taps of neighbouring voxels find them again.  Per-thread
+    // invariants (operand offsets, the voxel's row pointer, which of the three
+    // shifts per axis stay inside the volume) are computed once.
+    const bf16* vrow = in + (live ? v : 0) * cin;
+    const uint32_t zok = live ? (1u | 2u | 4u) & ~((z == 0 ? 1u : 0u) | (z == D - 1 ? 4u : 0u)) : 0u;
+    const uint32_t yok = (1u | 2u | 4u) & ~((y == 0 ? 1u : 0u) | (y == H - 1 ? 4u : 0u));
+    const uint32_t xok = (1u | 2u | 4u) & ~((x == 0 ? 1u : 0u) | (x == W - 1 ? 4u : 0u));
+    const uint32_t a_off0 = canon(tid, 0), a_off1 = canon(tid, 1);
+    int q_tap = 0, q_ks = 0;   // (tap, K step) of the next step to load; steps are loaded in order
     auto load_step = [&](int q, int s) {
-        const int tap = q / kc, ks = q - tap * kc;
+        const int tap = q_tap;
+        if (++q_ks == kc) { q_ks = 0; ++q_tap; }
         const uint32_t sa = smem0 + (uint32_t)s * stage_bytes;
         const uint32_t sb = sa + 4096u;
-        const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
-        const int zz = z + dz, yy = y + dy, xx = x + dx;
-        const bool in_range = live && zz >= 0 && zz < D && yy >= 0 && yy < H && xx >= 0 && xx < W;
-        const bf16* src = in_range ? in + ((((int64_t)n * D + zz) * H + yy) * W + xx) * cin + ks * 16 : in;
-        cp_async16_ca(sa + canon(tid, 0), src, in_range);
-        cp_async16_ca(sa + canon(tid, 1), src + 8, in_range);
-        for (int e = tid; e < COUT * 2; e += TC_THREADS) {
-            const int co = e >> 1, h = e & 1;
-            cp_async16_ca(sb + canon(co, h), w + ((int64_t)co * 27 + tap) * cin + ks * 16 + h * 8, true);
+        const int tz = tap / 9, ty = (tap / 3) % 3, tx = tap % 3;   // shift + 1 per axis
+        const bool in_range = (zok >> tz) & (yok >> ty) & (xok >> tx) & 1u;
+        const int64_t shift = ((int64_t)((tz - 1) * H + (ty - 1)) * W + (tx - 1)) * cin;
+        const bf16* src = in_range ? vrow + shift + (q - tap * kc) * 16 : in;
+        cp_async16_ca(sa + a_off0, src, in_range);
+        cp_async16_ca(sa + a_off1, src + 8, in_range);
+        // w[co][tap][ci]: tap * cin + 16 ks = 16 q
+#pragma unroll
+        for (int e0 = 0; e0 < COUT * 2; e0 += TC_THREADS) {
+            const int e = e0 + tid;
+            if (COUT * 2 % TC_THREADS == 0 || e < COUT * 2)
+                cp_async16_ca(sb + canon(e >> 1, e & 1), w + (int64_t)(e >> 1) * 27 * cin + (e & 1) * 8 + (int64_t)q * 16,
+                              true);
         }
     };
 
@@ -271,16 +284,17 @@ int launch_tc(const bf16* in, const bf16* w, const float* bias, const bf16* mask
 // WGT_CHUNK voxels, part[chunk][tap][co][ci] = sum_v g[v][co] * in[v + off][ci]
 // is a GEMM with M = co (TMEM lanes, rows >= cout stay zero), N = ci (TMEM
 // columns) and K = voxels.  g and in are channels-last, so each stage is
-// written into the K-major operand layout with a transposing store: a thread
-// loads 8 channels of one voxel (16 bytes) and stores them as 8 two-byte
-// elements of 8 operand rows.  The global loads of the next stage are issued
-// before the stores of the current one.  Partials are summed over chunks in a
+// written into the K-major operand layout with transposing 32-bit stores (two
+// voxels x one channel each; see the work units below).  The global loads of
+// the next stage are issued before the stores of the current one, and each
+// unit's voxel coordinates advance incrementally instead of being divided out
+// per stage.  Partials are summed over chunks in a
 // fixed order by wgrad_reduce_kernel (nn_unet.cu).  The CTAs of the centre
 // tap (no shift) also sum g over their chunk from the same loads: the bias
 // gradient partials dbpart[chunk][co].
 constexpr int WGT_CHUNK = 4096;
 constexpr int WGT_KV = 64;                 // voxels per stage (four K = 16 MMAs)
-constexpr int WGT_MAXA = 4, WGT_MAXB = 8;  // 16-byte loads per thread and stage (cout <= 64, cin <= 128)
+constexpr int WGT_UA = 2, WGT_UB = 4;      // work units per thread and stage (cout <= 64, cin <= 128)
 
 template <int CIN>
 __global__ void __launch_bounds__(TC_THREADS) conv3d_wgrad_tc_kernel(const bf16* __restrict__ in,
@@ -301,10 +315,12 @@ __global__ void __launch_bounds__(TC_THREADS) conv3d_wgrad_tc_kernel(const bf16*
     __shared__ float s_db[64];
 
     const int tid = threadIdx.x, warp = tid >> 5;
-    const int tap = blockIdx.y;
+    // the 27 taps of one chunk are consecutive CTAs, so g and the input chunk are read from L2
+    const int tap = blockIdx.x;
+    const int64_t chunk = blockIdx.y;
     const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
     const int64_t nvox = (int64_t)N * D * H * W;
-    const int64_t c0 = (int64_t)blockIdx.x * WGT_CHUNK;
+    const int64_t c0 = chunk * WGT_CHUNK;
     const uint32_t smem0 = smem_u32(smem);
 
     // zero both stages once: A rows >= cout are never written
@@ -327,61 +343,111 @@ __global__ void __launch_bounds__(TC_THREADS) conv3d_wgrad_tc_kernel(const bf16*
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t taddr = s_taddr;
     const bool centre = tap == 13;
-    float dbacc[WGT_MAXA][8];
+    float dbacc[WGT_UA][8];
 #pragma unroll
-    for (int u = 0; u < WGT_MAXA; ++u)
+    for (int u = 0; u < WGT_UA; ++u)
 #pragma unroll
         for (int h = 0; h < 8; ++h) dbacc[u][h] = 0.f;
 
-    const int ga = WGT_KV * (cout / 8), gb = WGT_KV * (CIN / 8);   // (voxel, 8-channel group) pairs
-    uint4 ra[WGT_MAXA], rb[WGT_MAXB];
+    // Work units of a stage: (octet o of 8 voxels, 8-channel group c8, voxel pair p); a unit
+    // loads 8 channels of voxels 8o + 2p and 8o + 2p + 1 and stores them as 8 32-bit words
+    // (two K neighbours of one operand row).  Lanes 4g' + p of a warp rotate their 8 rows by
+    // g', so the 32 lanes of one store hit 32 different banks.
+    const int na = 4 * cout, nb = 4 * CIN;   // units per stage
+    // B units follow the A units in thread order (B unit e on thread (e + na) mod 128), so
+    // small layers spread over all 128 threads; lane bits 0-4 are unchanged (na % 32 == 0)
+    const int boff = na & (TC_THREADS - 1);
+    const int64_t vshift = ((int64_t)dz * H + dy) * W + dx;
+    const int rot = (tid >> 2) & 7;
+    uint4 ra[WGT_UA][2], rb[WGT_UB][2];
+    // coordinates of each B unit's first voxel, advanced by WGT_KV voxels per stage
+    int bx[WGT_UB], by[WGT_UB], bz[WGT_UB];
+#pragma unroll
+    for (int u = 0; u < WGT_UB; ++u) {
+        const int e = ((tid - boff) & (TC_THREADS - 1)) + u * TC_THREADS, gq = e >> 2;
+        int64_t v = c0 + (gq & 7) * 8 + 2 * (e & 3);
+        bx[u] = (int)(v % W);
+        v /= W;
+        by[u] = (int)(v % H);
+        bz[u] = (int)((v / H) % D);
+    }
+    auto inside = [&](int x, int y, int z) {
+        return (unsigned)(x + dx) < (unsigned)W && (unsigned)(y + dy) < (unsigned)H && (unsigned)(z + dz) < (unsigned)D;
+    };
     auto fetch = [&](int q) {   // stage q's global data into registers
         const int64_t s0 = c0 + (int64_t)q * WGT_KV;
+        const int64_t lim = min(nvox, c0 + (int64_t)WGT_CHUNK);
 #pragma unroll
-        for (int u = 0; u < WGT_MAXA; ++u) {
+        for (int u = 0; u < WGT_UA; ++u) {
             const int e = tid + u * TC_THREADS;
-            uint4 val = make_uint4(0u, 0u, 0u, 0u);
-            if (e < ga) {
-                const int j = e % WGT_KV, c8 = e / WGT_KV;
-                const int64_t v = s0 + j;
-                if (v < nvox && v < c0 + WGT_CHUNK) val = *reinterpret_cast<const uint4*>(g + v * cout + c8 * 8);
+            ra[u][0] = ra[u][1] = make_uint4(0u, 0u, 0u, 0u);
+            if (e < na) {
+                const int gq = e >> 2, c8 = gq >> 3;
+                const int64_t v = s0 + (gq & 7) * 8 + 2 * (e & 3);
+                const bf16* src = g + v * cout + c8 * 8;
+                if (v < lim) ra[u][0] = *reinterpret_cast<const uint4*>(src);
+                if (v + 1 < lim) ra[u][1] = *reinterpret_cast<const uint4*>(src + cout);
             }
-            ra[u] = val;
         }
 #pragma unroll
-        for (int u = 0; u < WGT_MAXB; ++u) {
-            const int e = tid + u * TC_THREADS;
-            uint4 val = make_uint4(0u, 0u, 0u, 0u);
-            if (e < gb) {
-                const int j = e % WGT_KV, c8 = e / WGT_KV;
-                const int64_t v = s0 + j;
-                if (v < nvox && v < c0 + WGT_CHUNK) {
-                    int64_t t = v;
-                    const int x = (int)(t % W) + dx;
-                    t /= W;
-                    const int y = (int)(t % H) + dy;
-                    t /= H;
-                    const int z = (int)(t % D) + dz;
-                    const int nn = (int)(t / D);
-                    if (z >= 0 && z < D && y >= 0 && y < H && x >= 0 && x < W)
-                        val = *reinterpret_cast<const uint4*>(in + ((((int64_t)nn * D + z) * H + y) * W + x) * CIN + c8 * 8);
+        for (int u = 0; u < WGT_UB; ++u) {
+            const int e = ((tid - boff) & (TC_THREADS - 1)) + u * TC_THREADS;
+            rb[u][0] = rb[u][1] = make_uint4(0u, 0u, 0u, 0u);
+            if (e < nb) {
+                const int gq = e >> 2, c8 = gq >> 3;
+                const int64_t v = s0 + (gq & 7) * 8 + 2 * (e & 3);
+                int x1 = bx[u] + 1, y1 = by[u], z1 = bz[u];
+                if (x1 == W) {
+                    x1 = 0;
+                    if (++y1 == H) {
+                        y1 = 0;
+                        if (++z1 == D) z1 = 0;
+                    }
+                }
+                const bf16* src = in + (v + vshift) * CIN + c8 * 8;
+                if (v < lim && inside(bx[u], by[u], bz[u])) rb[u][0] = *reinterpret_cast<const uint4*>(src);
+                if (v + 1 < lim && inside(x1, y1, z1)) rb[u][1] = *reinterpret_cast<const uint4*>(src + CIN);
+            }
+            // advance to the next stage
+            bx[u] += WGT_KV;
+            while (bx[u] >= W) {
+                bx[u] -= W;
+                if (++by[u] == H) {
+                    by[u] = 0;
+                    if (++bz[u] == D) bz[u] = 0;
                 }
             }
-            rb[u] = val;
         }
     };
-    // transposing store: element (row, k) of a K = 16 step at canon(row, k / 8) + (k % 8) * 2
-    auto put = [&](uint32_t base, uint32_t step_bytes, int j, int c8, const uint4& val) {
-        const uint32_t sub = base + (uint32_t)(j >> 4) * step_bytes;
-        const int k = j & 15;
-        const uint32_t off = (uint32_t)((k >> 3) * 128 + (k & 7) * 2);
-        const uint32_t w4[4] = {val.x, val.y, val.z, val.w};
+    // rotate the 8 BF16 elements of a 16-byte vector by `rot` positions: element h of the
+    // result is element (h + rot) & 7 of the input
+    auto rotate8 = [&](const uint4& a) {
+        const int wq = rot >> 1;
+        uint32_t w0 = a.x, w1 = a.y, w2 = a.z, w3 = a.w;
+        uint32_t r0 = wq == 0 ? w0 : (wq == 1 ? w1 : (wq == 2 ? w2 : w3));
+        uint32_t r1 = wq == 0 ? w1 : (wq == 1 ? w2 : (wq == 2 ? w3 : w0));
+        uint32_t r2 = wq == 0 ? w2 : (wq == 1 ? w3 : (wq == 2 ? w0 : w1));
+        uint32_t r3 = wq == 0 ? w3 : (wq == 1 ? w0 : (wq == 2 ? w1 : w2));
+        if (rot & 1) {
+            const uint32_t t0 = __funnelshift_r(r0, r1, 16), t1 = __funnelshift_r(r1, r2, 16);
+            const uint32_t t2 = __funnelshift_r(r2, r3, 16), t3 = __funnelshift_r(r3, r0, 16);
+            r0 = t0; r1 = t1; r2 = t2; r3 = t3;
+        }
+        return make_uint4(r0, r1, r2, r3);
+    };
+    // store a unit: rows c8*8 + ((hh + rot) & 7), K positions j0 and j0 + 1 of the stage
+    auto put = [&](uint32_t base, uint32_t step_bytes, int e, const uint4& va, const uint4& vb) {
+        const int gq = e >> 2, c8 = gq >> 3, j0 = (gq & 7) * 8 + 2 * (e & 3);
+        const uint32_t sub = base + (uint32_t)(j0 >> 4) * step_bytes + (uint32_t)c8 * 256u +
+                             (uint32_t)(((j0 & 15) >> 3) * 128 + (j0 & 7) * 2);
+        const uint4 a = rotate8(va), b = rotate8(vb);
+        const uint32_t wa[4] = {a.x, a.y, a.z, a.w}, wb[4] = {b.x, b.y, b.z, b.w};
 #pragma unroll
-        for (int h = 0; h < 8; ++h) {
-            const int row = c8 * 8 + h;
-            const uint16_t b16 = (uint16_t)(w4[h >> 1] >> ((h & 1) * 16));
-            const uint32_t addr = sub + (uint32_t)((row >> 3) * 256 + (row & 7) * 16) + off;
-            asm volatile("st.shared.u16 [%0], %1;" ::"r"(addr), "h"(b16) : "memory");
+        for (int hh = 0; hh < 8; ++hh) {
+            const uint32_t lo = (wa[hh >> 1] >> ((hh & 1) * 16)) & 0xFFFFu;
+            const uint32_t hi = (wb[hh >> 1] >> ((hh & 1) * 16)) & 0xFFFFu;
+            const uint32_t addr = sub + (uint32_t)(((hh + rot) & 7) * 16);
+            asm volatile("st.shared.u32 [%0], %1;" ::"r"(addr), "r"(lo | (hi << 16)) : "memory");
         }
     };
 
@@ -397,22 +463,25 @@ __global__ void __launch_bounds__(TC_THREADS) conv3d_wgrad_tc_kernel(const bf16*
         }
         const uint32_t sa = smem0 + (uint32_t)s * STAGE, sb = sa + KS * A_STEP;
 #pragma unroll
-        for (int u = 0; u < WGT_MAXA; ++u) {
+        for (int u = 0; u < WGT_UA; ++u) {
             const int e = tid + u * TC_THREADS;
-            if (e < ga) {
-                put(sa, A_STEP, e % WGT_KV, e / WGT_KV, ra[u]);
+            if (e < na) {
+                put(sa, A_STEP, e, ra[u][0], ra[u][1]);
                 if (centre) {
-                    const uint32_t w4[4] = {ra[u].x, ra[u].y, ra[u].z, ra[u].w};
 #pragma unroll
-                    for (int h = 0; h < 8; ++h)
-                        dbacc[u][h] += __uint_as_float((w4[h >> 1] >> ((h & 1) * 16)) << 16);
+                    for (int h = 0; h < 8; ++h) {
+                        const uint32_t w0 = (h >> 1) == 0 ? ra[u][0].x : ((h >> 1) == 1 ? ra[u][0].y : ((h >> 1) == 2 ? ra[u][0].z : ra[u][0].w));
+                        const uint32_t w1 = (h >> 1) == 0 ? ra[u][1].x : ((h >> 1) == 1 ? ra[u][1].y : ((h >> 1) == 2 ? ra[u][1].z : ra[u][1].w));
+                        dbacc[u][h] += __uint_as_float((w0 >> ((h & 1) * 16)) << 16) +
+                                       __uint_as_float((w1 >> ((h & 1) * 16)) << 16);
+                    }
                 }
             }
         }
 #pragma unroll
-        for (int u = 0; u < WGT_MAXB; ++u) {
-            const int e = tid + u * TC_THREADS;
-            if (e < gb) put(sb, B_STEP, e % WGT_KV, e / WGT_KV, rb[u]);
+        for (int u = 0; u < WGT_UB; ++u) {
+            const int e = ((tid - boff) & (TC_THREADS - 1)) + u * TC_THREADS;
+            if (e < nb) put(sb, B_STEP, e, rb[u][0], rb[u][1]);
         }
         if (q + 1 < nq) fetch(q + 1);
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -428,17 +497,17 @@ __global__ void __launch_bounds__(TC_THREADS) conv3d_wgrad_tc_kernel(const bf16*
     }
     if (tid == 0) tc_commit(&s_bar[2]);
     if (centre) {   // bias-gradient partial of this chunk: fixed-order shared reduction
-        for (int j0 = 0; j0 < WGT_KV; ++j0) {
+        for (int slot = 0; slot < 32; ++slot) {   // (octet, pair) = (slot >> 2, slot & 3)
 #pragma unroll
-            for (int u = 0; u < WGT_MAXA; ++u) {
+            for (int u = 0; u < WGT_UA; ++u) {
                 const int e = tid + u * TC_THREADS;
-                if (e < ga && e % WGT_KV == j0)
+                if (e < na && (((e >> 2) & 7) << 2 | (e & 3)) == slot)
 #pragma unroll
-                    for (int h = 0; h < 8; ++h) s_db[(e / WGT_KV) * 8 + h] += dbacc[u][h];
+                    for (int h = 0; h < 8; ++h) s_db[(e >> 5) * 8 + h] += dbacc[u][h];
             }
             __syncthreads();
         }
-        if (tid < cout) dbpart[(int64_t)blockIdx.x * cout + tid] = s_db[tid];
+        if (tid < cout) dbpart[chunk * cout + tid] = s_db[tid];
     }
     if (!mbar_wait(&s_bar[2], 0)) s_fail = 1;
     __syncthreads();
@@ -446,7 +515,7 @@ __global__ void __launch_bounds__(TC_THREADS) conv3d_wgrad_tc_kernel(const bf16*
     if (!s_fail) {
         if (warp * 32 < cout) {
             const int co = warp * 32 + (tid & 31);
-            float* dst = part + (((int64_t)blockIdx.x * 27 + tap) * cout + co) * CIN;
+            float* dst = part + ((chunk * 27 + tap) * cout + co) * CIN;
 #pragma unroll
             for (int c = 0; c < CIN; c += 16) {
                 float acc[16];
@@ -505,13 +574,15 @@ int lbm_nn_tc_status(int32_t* timed_out) {
 
 }  // extern "C"
 
-// Tensor-core weight-gradient partials (see conv3d_wgrad_tc_kernel); grid (chunks, 27).
+// Tensor-core weight-gradient partials (see conv3d_wgrad_tc_kernel); grid (27 taps, chunks).
 int nn_wgrad_tc_launch(const void* in, const void* g, float* part, float* dbpart, int n, int d, int h, int w, int cin,
                        int cout, cudaStream_t s) {
     if (cin % 16 || cin < 16 || cin > 128 || cout % 8 || cout < 8 || cout > 64)
         return lbm_set_err(nullptr, LBM_EINVAL, "lbm_nn_conv3d_wgrad: cin must be a multiple of 16 up to 128, cout a multiple of 8 up to 64");
     const int64_t nvox = (int64_t)n * d * h * w;
-    const dim3 grid((unsigned)((nvox + WGT_CHUNK - 1) / WGT_CHUNK), 27);
+    if ((nvox + WGT_CHUNK - 1) / WGT_CHUNK > 65535)
+        return lbm_set_err(nullptr, LBM_EINVAL, "lbm_nn_conv3d_wgrad: more than 65535 x 4096 voxels");
+    const dim3 grid(27, (unsigned)((nvox + WGT_CHUNK - 1) / WGT_CHUNK));
     const size_t smem = 2 * (WGT_KV / 16) * (4096 + (size_t)cin * 32);
 #define LBM_WG(C)                                                                                              \
     case C: {                                                                                                  \

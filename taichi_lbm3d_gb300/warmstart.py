@@ -1,6 +1,6 @@
 """Learned warm start: dataset generation, training and the rest-vs-warm evaluation.
 
-    python -m taichi_lbm3d_gb300.warmstart --train-n 2000 --edge 96 --epochs 6 \\
+    python -m taichi_lbm3d_gb300.warmstart --train-n 2000 --edge 96 --epochs 12 \\
         --eval-n 100 --eval-edge 192 --fp64-subset 4 --out weights.npz --report report.json
 
 1. Training data: seeded sphere packs (edge ``--edge``, radii U[3,8], porosity
@@ -11,10 +11,12 @@
    (v, rho - 1), masked MSE on fluid voxels, Adam; all forward/backward work in
    the project's CUDA kernels.
 3. Evaluation on held-out packs (edge ``--eval-edge``): steps and wall time to
-   the same convergence criterion (a) for the plain FP32 kernel from rest and
+   the same convergence criterion (a) for the plain FP32 kernel from rest,
    (b) for FP16 storage started from the network's prediction (inference and
-   initialisation included), and the permeability of both against the FP64
-   run of the same solver on a subset.
+   initialisation included), (c) the same with the predicted velocity only
+   (rho = 1) and (d) FP16 storage from rest, which separates what the network
+   gains from what the storage gains; and the permeability of each against the
+   FP64 run of the same solver on a subset.
 """
 import argparse
 import json
@@ -158,6 +160,14 @@ def evaluate(model, solids, feats, fp64_subset=4, log=print):
         row.update(warm_f16_steps=r["steps"], warm_f16_seconds=time.perf_counter() - t, warm_f16_k=r["k"],
                    inference_and_init_seconds=t_inf)
         lb.close()
+        # the same prediction with rho = 1: velocity only
+        t = time.perf_counter()
+        lb = _solver(s, "f16")
+        lb.init_simulation(np.ones_like(rho), v)
+        r = lb.run_to_convergence()
+        row.update(warm_v_f16_steps=r["steps"], warm_v_f16_seconds=time.perf_counter() - t + t_inf,
+                   warm_v_f16_k=r["k"])
+        lb.close()
         lb = _solver(s, "f16")
         lb.init_simulation()
         t = time.perf_counter()
@@ -170,14 +180,15 @@ def evaluate(model, solids, feats, fp64_subset=4, log=print):
             t = time.perf_counter()
             r = lb.run_to_convergence()
             row.update(f64_k=r["k"], f64_steps=r["steps"], f64_seconds=time.perf_counter() - t)
-            for key in ("rest_f32", "warm_f16", "rest_f16"):
+            for key in ("rest_f32", "warm_f16", "warm_v_f16", "rest_f16"):
                 row[key + "_k_err"] = abs(row[key + "_k"] - r["k"]) / abs(r["k"])
             lb.close()
         row["speedup_warm_f16_vs_rest_f32"] = row["rest_f32_seconds"] / row["warm_f16_seconds"]
         row["step_ratio_warm_vs_rest_f16"] = row["rest_f16_steps"] / max(1, row["warm_f16_steps"])
-        log("eval %d: rest f32 %d steps %.2f s | warm f16 %d steps %.2f s | rest f16 %d steps" % (
+        row["step_ratio_warm_v_vs_rest_f16"] = row["rest_f16_steps"] / max(1, row["warm_v_f16_steps"])
+        log("eval %d: rest f32 %d steps %.2f s | warm f16 %d steps %.2f s | warm v-only f16 %d | rest f16 %d steps" % (
             q, row["rest_f32_steps"], row["rest_f32_seconds"], row["warm_f16_steps"], row["warm_f16_seconds"],
-            row["rest_f16_steps"]))
+            row["warm_v_f16_steps"], row["rest_f16_steps"]))
         rows.append(row)
     return rows
 
@@ -198,8 +209,15 @@ def summarize(rows):
             "steps_rest_f32_median": med("rest_f32_steps"), "steps_warm_f16_median": med("warm_f16_steps"),
             "steps_rest_f16_median": med("rest_f16_steps"),
             "step_ratio_rest_over_warm_f16_median": med("step_ratio_warm_vs_rest_f16"),
+            "step_ratio_rest_over_warm_f16_mean": float(np.mean([r["step_ratio_warm_vs_rest_f16"] for r in rows])),
+            "steps_warm_v_f16_median": med("warm_v_f16_steps"),
+            "step_ratio_rest_over_warm_v_f16_mean": float(np.mean([r["step_ratio_warm_v_vs_rest_f16"] for r in rows])),
+            "warm_fewer_steps": int(sum(r["warm_f16_steps"] < r["rest_f16_steps"] for r in rows)),
+            "warm_more_steps": int(sum(r["warm_f16_steps"] > r["rest_f16_steps"] for r in rows)),
+            "warm_v_fewer_steps": int(sum(r["warm_v_f16_steps"] < r["rest_f16_steps"] for r in rows)),
+            "warm_v_more_steps": int(sum(r["warm_v_f16_steps"] > r["rest_f16_steps"] for r in rows)),
             "k_err_warm_f16_vs_f64_max": mx("warm_f16_k_err"), "k_err_rest_f32_vs_f64_max": mx("rest_f32_k_err"),
-            "k_err_rest_f16_vs_f64_max": mx("rest_f16_k_err")}
+            "k_err_rest_f16_vs_f64_max": mx("rest_f16_k_err"), "k_err_warm_v_f16_vs_f64_max": mx("warm_v_f16_k_err")}
 
 
 def main(argv=None):
@@ -207,7 +225,7 @@ def main(argv=None):
     ap.add_argument("--train-n", type=int, default=2000)
     ap.add_argument("--edge", type=int, default=96)
     ap.add_argument("--train-seed0", type=int, default=10000)
-    ap.add_argument("--epochs", type=int, default=6)
+    ap.add_argument("--epochs", type=int, default=12)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--eval-n", type=int, default=100)
     ap.add_argument("--eval-edge", type=int, default=192)
