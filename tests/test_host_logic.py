@@ -87,3 +87,39 @@ def test_max_over_ranks_gloo_world2():
     for p in ps:
         p.join(timeout=60)
     assert got == {0: 2.0, 1: 2.0}
+
+
+def test_grey_class_parameters_and_geometry_file(tmp_path):
+    """The grey-scale class maps the script's globals onto the C parameters:
+    tau = 3 niu + 1/2 and the script's Guo form, in-place velocity faces, and
+    x faces only (the script's y/z settings have no effect)."""
+    from taichi_lbm3d_gb300 import LB3D_Solver_Grey_Scale
+    lb = LB3D_Solver_Grey_Scale(6, 5, 4)
+    assert (lb.fx, lb.niu, lb.bc_x_left, lb.rho_bcxr) == (1.0e-6, 0.1, 0, 0.995)   # script defaults
+    lb.bc_x_left, lb.rho_bcxl = 1, 1.002
+    lb.bc_x_right, lb.vx_bcxr = 2, 0.01
+    lb.bc_y_left = 1                                     # ignored, as in the script
+    p = lb._params()
+    assert list(p.bc) == [1, 2, 0, 0, 0, 0]
+    assert p.rho_bc[0] == 1.002 and p.vel_bc[1][0] == 0.01
+    assert (p.visc_convention, p.guo_convention, p.bc_form) == (1, 1, 1)
+    assert tuple(p.force) == (1.0e-6, 0.0, 0.0)
+    # geometry file: x fastest, float64 like np.loadtxt; solid = ns.astype(int)
+    ns = np.zeros((6, 5, 4))
+    ns[:, 0, :] = 1.0
+    ns[2:4, 2, 1] = 0.2
+    path = tmp_path / "BC.dat"
+    np.savetxt(path, ns.ravel(order="F"))
+    got = lb.load_geo(str(path))
+    assert got.dtype == np.float64 and np.array_equal(got, ns)
+    assert np.array_equal(lb.solid.to_numpy(), ns.astype(int)) and np.array_equal(lb.ns.to_numpy(), ns)
+
+
+def test_voxelize_cli_rejects_missing_file(tmp_path):
+    from taichi_lbm3d_gb300 import voxelize as vx
+    with pytest.raises(OSError):
+        vx.main([str(tmp_path / "absent.stl")])
+    bad = tmp_path / "bad.stl"
+    bad.write_text("not a mesh")
+    with pytest.raises(ValueError):
+        vx.read_stl(str(bad))
