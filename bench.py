@@ -179,9 +179,8 @@ def e2e_run(solid, steps):
     secs = time.perf_counter() - t0
     nf = lb.n_fluid
     lb.close()
-    np_pad = (nf + 63) // 64 * 64
-    h2d = solid.size * 1 + 4 * solid.size + 4 * np_pad          # mask, neighbour map, coordinates
-    d2h = 16 * np_pad                                            # rho + v of the fluid nodes
+    h2d = solid.size * 1                                         # the int8 mask (index built on the device)
+    d2h = 16 * solid.size                                        # dense rho + v (scattered on the device)
     assert np.isfinite(rho).all() and np.isfinite(v).all()
     return nf * steps / secs / 1e6, h2d / steps, d2h / steps
 
