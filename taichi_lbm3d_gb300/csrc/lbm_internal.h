@@ -25,6 +25,9 @@ struct SpConsts {
     R sv, so;          // S_dig values s_v, s_other (SP:128-131)
     R fext[3];
     R fhalf[3];        // fext / 2 (SP:388)
+    // Deviation-form kernels: moments of the Guo term in closed form, M (w o g)
+    // with g = gc (e - u).F + gd (e.u)(e.F); the (gc, gd) of the convention
+    R gc, gd;
 };
 
 struct LbmHandle {

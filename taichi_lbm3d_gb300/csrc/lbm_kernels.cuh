@@ -146,7 +146,32 @@ __device__ __forceinline__ void collide_sp(R* F, R r, R vx, R vy, R vz, const Sp
         if constexpr (FAST) m[s] = lbm_fma<R>(S, meq[s] - m[s], m[s]);
         else m[s] = m[s] - S * (m[s] - meq[s]);
     }
-    if constexpr (FORCE) {
+    if constexpr (FORCE && FAST) {
+        // M (w o g) in closed form, from sum_l M_rl w_l, sum_l M_rl w_l e_l and
+        // sum_l M_rl w_l e_l e_l^T of this M (checked in tests/test_host_tables.py):
+        // moment 0: (gd/3 - gc) u.F,
+        // moment 1: 2/9 gd u.F, moments 3, 5, 7: gc F / 3, moment 9:
+        // gd (4 ux Fx - 2 uy Fy - 2 uz Fz) / 9, moment 11: 2/9 gd (uy Fy - uz Fz),
+        // moments 13, 14, 15: gd (ua Fb + ub Fa) / 9; the others vanish.  Moments
+        // 0, 3, 5, 7 are conserved (S = 0); 1, 9, 11, 13-15 relax with s_v.
+        const R fx = C.fext[0], fy = C.fext[1], fz = C.fext[2];
+        const R gc = C.gc, gd = C.gd;
+        const R ksv = (R)1 - (R)0.5 * C.sv;
+        const R uf = lbm_fma<R>(vz, fz, lbm_fma<R>(vy, fy, vx * fx));
+        const R d9 = gd * (R)(1.0 / 9.0);
+        m[0] = lbm_fma<R>(gd * (R)(1.0 / 3.0) - gc, uf, m[0]);
+        m[1] = lbm_fma<R>(ksv * (R)2 * d9, uf, m[1]);
+        const R c3 = gc * (R)(1.0 / 3.0);
+        m[3] = lbm_fma<R>(c3, fx, m[3]);
+        m[5] = lbm_fma<R>(c3, fy, m[5]);
+        m[7] = lbm_fma<R>(c3, fz, m[7]);
+        const R kd9 = ksv * d9;
+        m[9] = lbm_fma<R>(kd9, (R)4 * (vx * fx) - (R)2 * lbm_fma<R>(vy, fy, vz * fz), m[9]);
+        m[11] = lbm_fma<R>(kd9 * (R)2, lbm_fma<R>(vy, fy, -(vz * fz)), m[11]);
+        m[13] = lbm_fma<R>(kd9, lbm_fma<R>(vx, fy, vy * fx), m[13]);
+        m[14] = lbm_fma<R>(kd9, lbm_fma<R>(vy, fz, vz * fy), m[14]);
+        m[15] = lbm_fma<R>(kd9, lbm_fma<R>(vx, fz, vz * fx), m[15]);
+    } else if constexpr (FORCE) {
         const R fx = C.fext[0], fy = C.fext[1], fz = C.fext[2];
         R G[19];
 #pragma unroll
@@ -168,14 +193,12 @@ __device__ __forceinline__ void collide_sp(R* F, R r, R vx, R vy, R vz, const Sp
             G[l] = (R)lbm_w(l) * g;
         }
         R fg[19];
-        if constexpr (FAST) mrt_moments_fast<R>(G, fg);
-        else mrt_moments<R>(G, fg);
+        mrt_moments<R>(G, fg);
 #pragma unroll
         for (int s = 0; s < 19; ++s) {
             const int kd = lbm_skind(s);
             const R S = kd == 0 ? (R)0 : (kd == 1 ? C.sv : C.so);
-            if constexpr (FAST) m[s] = lbm_fma<R>((R)1 - (R)0.5 * S, fg[s], m[s]);
-            else m[s] = m[s] + ((R)1 - (R)0.5 * S) * fg[s];
+            m[s] = m[s] + ((R)1 - (R)0.5 * S) * fg[s];
         }
     }
     if constexpr (FAST) mrt_back_fast<R>(m, F);

@@ -205,6 +205,9 @@ SpConsts<R> sp_make_consts(const LbmHandle* h) {
         C.fext[c] = (R)p.force[c];
         C.fhalf[c] = C.fext[c] / (R)2;
     }
+    // class (SP:236): /3, /9; scripts (TP:246): 1, 1; standard Guo: 3, 9
+    C.gc = p.guo_convention == 0 ? (R)(1.0 / 3.0) : (p.guo_convention == 1 ? (R)1 : (R)3);
+    C.gd = p.guo_convention == 0 ? (R)(1.0 / 9.0) : (p.guo_convention == 1 ? (R)1 : (R)9);
     return C;
 }
 template SpConsts<float> sp_make_consts<float>(const LbmHandle*);

@@ -189,6 +189,26 @@ def test_reductions_match_host_sums():
 # Transient (300 steps from rest) error of the deviation-storage variants,
 # normwise against the FP64 oracle: FP16 keeps 11 significant bits of f - w,
 # BF16 8; FP64 must agree to round-off.
+@pytest.mark.parametrize("storage,tol", [("f32dev", 1e-4), ("f16", 2e-2), ("bf16", 1e-1)])
+@pytest.mark.parametrize("guo", [0, 1, 2])
+def test_forced_storage_variants_close_to_fp64_oracle(storage, tol, guo):
+    """Body-force runs: the deviation-form kernels add the Guo moments in
+    closed form; every convention stays within the storage's tolerance of the
+    FP64 oracle's dense form."""
+    solid = sphere_pack((32, 24, 24), 2.5, 5, 0.45, seed=19)
+    p = oracle_params((32, 24, 24), niu=0.1, force=(2e-5, -1e-5, 5e-6), visc_convention=1, guo_convention=guo)
+    o = Oracle(p, solid, precision=64)
+    o.step(300)
+    lat = lattice(p, solid, storage=storage)
+    lat.step(300)
+    rho, v = lat.macros_f64()
+    fl = solid == 0
+    e_rho = np.abs(rho[fl] - o.field("rho")[fl]).max() / max(np.abs(o.field("rho")[fl] - 1.0).max(), 1e-30)
+    e_v = G.normwise_rel(v, o.field("v"), fl)
+    print("forced storage %s guo %d: e_rho %.3e e_v %.3e" % (storage, guo, e_rho, e_v))
+    assert e_v < tol and e_rho < max(tol, 1e-3), (storage, guo, e_rho, e_v)
+
+
 @pytest.mark.parametrize("storage,tol", [("f64", 1e-9), ("f32dev", 1e-4), ("f16", 2e-2), ("bf16", 1e-1)])
 def test_storage_variants_close_to_fp64_oracle(storage, tol):
     solid = sphere_pack((32, 24, 24), 2.5, 5, 0.45, seed=9)
