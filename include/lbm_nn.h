@@ -28,6 +28,10 @@ int lbm_nn_conv3d(const void* in, const void* w, const float* bias, const void* 
 /* *timed_out = 1 when a tensor-core convolution gave up waiting on its
  * pipeline since the last call (its output is then invalid); clears the flag. */
 int lbm_nn_tc_status(int32_t* timed_out);
+/* Self-test of that path: one CTA allocates tensor memory, waits (bounded,
+ * about 1e6 cycles) on an mbarrier phase that nothing completes, sets the flag,
+ * frees its tensor memory and returns; the context stays usable. */
+int lbm_nn_tc_timeout_selftest(void* stream);
 /* wt[ci][tap][co] = w[co][26 - tap][ci]: weights of the backward-data conv. */
 int lbm_nn_flip_transpose(const void* w, void* wt, int32_t cin, int32_t cout, void* stream);
 /* Weight gradient dw[co][tap][ci] (FP32) and bias gradient db[co] (may be NULL)

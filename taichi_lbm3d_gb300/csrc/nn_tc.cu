@@ -44,8 +44,8 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
 }
 
-// Wait for the phase with the given parity to complete; false after ~1 s.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// Wait for the phase with the given parity to complete; false after `limit` cycles (~1 s).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long limit = TC_WAIT_CYCLES) {
     const long long t0 = clock64();
     for (;;) {
         uint32_t done;
@@ -55,7 +55,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
             : "r"(smem_u32(bar)), "r"(parity)
             : "memory");
         if (done) return true;
-        if (clock64() - t0 > TC_WAIT_CYCLES) return false;
+        if (clock64() - t0 > limit) return false;
     }
 }
 
@@ -277,6 +277,31 @@ int launch_tc(const bf16* in, const bf16* w, const float* bias, const bf16* mask
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return lbm_set_err(nullptr, LBM_ECUDA, std::string("conv3d_tc_kernel: ") + cudaGetErrorString(e));
     return LBM_OK;
+}
+
+// Self-test of the timeout path: one CTA allocates tensor memory, waits on an
+// mbarrier whose phase nothing completes (no arrival is ever made) with a
+// short bound, records the timeout in the error flag exactly as the
+// convolution kernels do, frees its tensor memory and returns.
+__global__ void __launch_bounds__(32) tc_timeout_selftest_kernel(long long limit) {
+    __shared__ uint64_t s_bar;
+    __shared__ uint32_t s_taddr;
+    if (threadIdx.x == 0) {
+        mbar_init(&s_bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&s_taddr)), "r"(32)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t taddr = s_taddr;
+    const bool done = mbar_wait(&s_bar, 0, limit);
+    if (!done && threadIdx.x == 0) atomicExch(&g_tc_error, 1);
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(32) : "memory");
 }
 
 // ---------------------------------------------------------------------------
@@ -559,6 +584,17 @@ int lbm_nn_conv3d(const void* in, const void* w, const float* bias, const void* 
         return lbm_set_err(nullptr, LBM_EINVAL, "lbm_nn_conv3d: cout must be 16, 32, 48, 64 or 96");
     }
 #undef LBM_TC
+}
+
+// Runs the timeout self-test (about 1e6 cycles of waiting on a barrier nothing
+// completes) and waits for it; the flag it sets is read with lbm_nn_tc_status.
+int lbm_nn_tc_timeout_selftest(void* stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    tc_timeout_selftest_kernel<<<1, 32, 0, s>>>(1000000LL);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return lbm_set_err(nullptr, LBM_ECUDA, std::string("tc_timeout_selftest: ") + cudaGetErrorString(e));
+    return LBM_OK;
 }
 
 // 0 when no tensor-core convolution has timed out since the last call; clears the flag.

@@ -31,6 +31,7 @@ _F = ctypes.c_float
 _SIGS = {
     "lbm_nn_conv3d": ([_P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _I, _P], ctypes.c_int),
     "lbm_nn_tc_status": ([_P], ctypes.c_int),
+    "lbm_nn_tc_timeout_selftest": ([_P], ctypes.c_int),
     "lbm_nn_flip_transpose": ([_P, _P, _I, _I, _P], ctypes.c_int),
     "lbm_nn_wgrad_scratch_floats": ([_I, _I, _I, _I, _I, _I], ctypes.c_int64),
     "lbm_nn_conv3d_wgrad": ([_P, _P, _P, _P, _P, _L, _I, _I, _I, _I, _I, _I, _P], ctypes.c_int),

@@ -78,3 +78,18 @@ def test_tc_weight_gradient_matches_reference(cin, cout):
     e_w = np.abs(dw.cpu().numpy() - dw_ref).max() / np.abs(dw_ref).max()
     e_b = np.abs(db.cpu().numpy() - db_ref).max() / np.abs(db_ref).max()
     assert e_w < 1e-4 and e_b < 1e-4, (e_w, e_b)
+
+
+def test_tc_wait_timeout_sets_the_flag_and_keeps_the_context():
+    """The bounded mbarrier wait gives up on a phase that nothing completes,
+    records it, frees its tensor memory and returns; later work still runs."""
+    import torch
+    from taichi_lbm3d_gb300 import unet
+    L = unet._lib()
+    flag = ctypes.c_int32(0)
+    assert L.lbm_nn_tc_status(ctypes.byref(flag)) == 0          # clear
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert L.lbm_nn_tc_timeout_selftest(s) == 0
+    assert L.lbm_nn_tc_status(ctypes.byref(flag)) == 0 and flag.value == 1
+    assert L.lbm_nn_tc_status(ctypes.byref(flag)) == 0 and flag.value == 0   # cleared by the read
+    test_tc_conv_matches_reference(16, 16, 0)                               # the context still works
