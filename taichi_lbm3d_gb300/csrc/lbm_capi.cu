@@ -16,6 +16,64 @@
 
 namespace {
 std::mutex g_err_mu;
+
+// L2 residency of the neighbour map.  The 18 map lookups of every node sit on
+// the step's critical path (coordinates -> map -> populations) and the map
+// (4 B per cell) is otherwise evicted by the populations streaming through L2
+// every step.  Each handle marks its map as a persisting access-policy window
+// on its stream; the process-wide set-aside (a limit of this process's CUDA
+// context, released when the process exits) is the largest map in use, capped
+// at the device maximum, and is returned to 0 when the last handle on the
+// device that used it is destroyed.  Best effort: failures only skip it.
+std::mutex g_l2_mu;
+int g_l2_users[64];
+size_t g_l2_size[64];
+
+void l2_persist_map(LbmHandle* h) {
+    if (h->device < 0 || h->device >= 64 || !h->d_map) return;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, h->device) != cudaSuccess || prop.persistingL2CacheMaxSize <= 0 ||
+        prop.accessPolicyMaxWindowSize <= 0) {
+        cudaGetLastError();
+        return;
+    }
+    const size_t map_bytes = sizeof(int32_t) * (size_t)h->ncell;
+    const size_t want = std::min<size_t>(map_bytes, (size_t)prop.persistingL2CacheMaxSize);
+    {
+        std::lock_guard<std::mutex> lk(g_l2_mu);
+        if (want > g_l2_size[h->device]) {
+            if (cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, want) != cudaSuccess) {
+                cudaGetLastError();
+                return;
+            }
+            g_l2_size[h->device] = want;
+        }
+        ++g_l2_users[h->device];
+    }
+    cudaStreamAttrValue attr = {};
+    attr.accessPolicyWindow.base_ptr = (void*)h->d_map;
+    attr.accessPolicyWindow.num_bytes = std::min<size_t>(map_bytes, (size_t)prop.accessPolicyMaxWindowSize);
+    attr.accessPolicyWindow.hitRatio = std::min(1.0f, (float)want / (float)attr.accessPolicyWindow.num_bytes);
+    attr.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+    attr.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+    if (cudaStreamSetAttribute(h->stream, cudaStreamAttributeAccessPolicyWindow, &attr) != cudaSuccess) cudaGetLastError();
+    h->l2_persist = true;
+}
+
+void l2_release(LbmHandle* h) {
+    if (!h->l2_persist) return;
+    h->l2_persist = false;
+    cudaStreamAttrValue attr = {};
+    attr.accessPolicyWindow.num_bytes = 0;   // clear the window
+    if (h->stream && cudaStreamSetAttribute(h->stream, cudaStreamAttributeAccessPolicyWindow, &attr) != cudaSuccess)
+        cudaGetLastError();
+    std::lock_guard<std::mutex> lk(g_l2_mu);
+    if (--g_l2_users[h->device] == 0) {
+        if (cudaCtxResetPersistingL2Cache() != cudaSuccess) cudaGetLastError();
+        if (cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, 0) != cudaSuccess) cudaGetLastError();
+        g_l2_size[h->device] = 0;
+    }
+}
 std::string g_err;
 
 int set_global_err(int code, const std::string& m) {
@@ -173,6 +231,7 @@ int lbm_destroy(LbmHandle* h) {
     if (!h) return LBM_OK;
     cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
+    l2_release(h);
     free_lattice(h);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
@@ -188,6 +247,7 @@ int lbm_set_geometry_strided(LbmHandle* h, const int8_t* solid, int64_t si, int6
     if (si < 0 || sj < 0 || sk < 0) return lbm_set_err(h, LBM_EINVAL, "lbm_set_geometry: negative stride");
     cudaSetDevice(h->device);
     cudaStreamSynchronize(h->stream);
+    l2_release(h);
     free_lattice(h);
     h->have_geometry = h->initialized = h->macros_valid = false;
     int rc = geom_build(h, solid, si, sj, sk);
@@ -221,6 +281,7 @@ int lbm_set_geometry_strided(LbmHandle* h, const int8_t* solid, int64_t si, int6
     if (rc) { free_lattice(h); return rc; }
     h->have_geometry = true;
     h->have_psi = false;
+    l2_persist_map(h);
     return LBM_OK;
 }
 

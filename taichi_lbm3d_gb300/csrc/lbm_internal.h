@@ -48,6 +48,7 @@ struct LbmHandle {
     std::vector<int8_t> solid;             // dense host copy (made on demand: geom_host_index)
     std::vector<int32_t> cell_of_node;     // n_fluid (made on demand)
     bool host_index_valid = false;
+    bool l2_persist = false;               // the map is this stream's persisting L2 window
     std::vector<float> psi0;               // dense initial psi (two phase)
 
     int32_t* d_map = nullptr;              // dense: node index or -1 (solid)
