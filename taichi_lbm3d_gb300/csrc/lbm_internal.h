@@ -53,7 +53,7 @@ struct LbmHandle {
 
     int32_t* d_map = nullptr;              // dense: node index or -1 (solid)
     uint32_t* d_coord = nullptr;           // packed (i,j,k) per node
-    void* d_f[2] = {nullptr, nullptr};     // populations [19][np]
+    void* d_f[2] = {nullptr, nullptr};     // populations, 19 x np elements in AoSoA-32 chunks
     int cur = 0;
     void* d_vprev = nullptr;               // [3][np] previous-step v (pressure faces)
     void* d_rho = nullptr;                 // [np]

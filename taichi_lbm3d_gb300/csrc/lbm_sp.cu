@@ -10,11 +10,13 @@
 //   collide  m = M F; m -= S (m - meq); Guo term; f = M^-1 m (colission, SP:222-241)
 // Paths: SP = Single_phase/LBM_3D_SinglePhase_Solver.py (taichi_LBM3D tree).
 //
-// Memory layout (HBM): populations SoA [19][np] in two buffers (ping-pong),
-// np = n_fluid padded to 64; dense int32 map cell -> node (or -1 for solid);
-// packed node coordinates.  Per node and step the kernel moves 19 loads + 19
-// stores of populations (152 B in FP32, 76 B in 16-bit storage), 4 B of
-// coordinates and the neighbour map rows (mostly L1/L2 hits).
+// Memory layout (HBM): populations in AoSoA-32 chunks (element (n, s) at
+// n + (n >> 5) * 576 + 32 s, lbm_common.cuh) in two buffers (ping-pong),
+// np = n_fluid padded to 64; dense int32 map cell -> node (or -1 for solid),
+// kept L2-resident by a persisting access-policy window (lbm_capi.cu); packed
+// node coordinates.  Per node and step the kernel moves 19 loads + 19 stores
+// of populations (152 B in FP32, 76 B in 16-bit storage), 4 B of coordinates
+// and the neighbour map rows (L1/L2 hits).
 #include <cuda_runtime.h>
 
 #include "lbm_common.cuh"
