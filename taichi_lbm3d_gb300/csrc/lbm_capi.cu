@@ -50,10 +50,13 @@ void l2_persist_map(LbmHandle* h) {
         }
         ++g_l2_users[h->device];
     }
+    // A window no larger than the set-aside, all of it persisting: for maps larger
+    // than the set-aside only their first part persists (a window wider than the
+    // set-aside with a fractional hit ratio made the persisting lines thrash).
     cudaStreamAttrValue attr = {};
     attr.accessPolicyWindow.base_ptr = (void*)h->d_map;
-    attr.accessPolicyWindow.num_bytes = std::min<size_t>(map_bytes, (size_t)prop.accessPolicyMaxWindowSize);
-    attr.accessPolicyWindow.hitRatio = std::min(1.0f, (float)want / (float)attr.accessPolicyWindow.num_bytes);
+    attr.accessPolicyWindow.num_bytes = std::min<size_t>(want, (size_t)prop.accessPolicyMaxWindowSize);
+    attr.accessPolicyWindow.hitRatio = 1.0f;
     attr.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
     attr.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
     if (cudaStreamSetAttribute(h->stream, cudaStreamAttributeAccessPolicyWindow, &attr) != cudaSuccess) cudaGetLastError();
