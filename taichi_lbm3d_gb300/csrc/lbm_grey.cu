@@ -112,11 +112,16 @@ __global__ void __launch_bounds__(256, STORE == LBM_STORE_F64 ? 1 : 4) grey_step
     typename Codec<STORE>::R* __restrict__ v_out, const float* __restrict__ rref_in, float* __restrict__ rref_out) {
     using Cd = Codec<STORE>;
     using R = typename Cd::R;
+    // programmatic dependent launch, as in the single-phase step: the next
+    // step's CTAs may start once all of these run; they wait below before
+    // reading populations, grey values' partners or the face side array
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= C.n_fluid) return;
     const uint32_t pc = __ldg(coord + n);
     const int i = lbm_pi(pc), j = lbm_pj(pc), k = lbm_pk(pc);
     const int64_t np = C.np;
+    asm volatile("griddepcontrol.wait;" ::: "memory");
 
     R F[19];
     grey_gather_node<STORE>(F, fin, map, ns, n, C.nx, C.ny, C.nz, i, j, k, rref_in);
@@ -175,11 +180,21 @@ int launch_grey(LbmHandle* h, const SpConsts<typename Codec<STORE>::R>& C, int g
     using R = typename Codec<STORE>::R;
     const T* fin = (const T*)h->d_f[h->cur];
     T* fout = (T*)h->d_f[h->cur ^ 1];
-    grey_step_kernel<STORE, FORCE, MACROS><<<grid, h->block, 0, h->stream>>>(
-        C, fin, fout, h->d_map, h->d_coord, (const R*)h->d_ns, (R*)h->d_gstale, (R*)h->d_vprev, (R*)h->d_rho,
-        (R*)h->d_v, h->d_rref[h->cur], h->d_rref[h->cur ^ 1]);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)h->block);
+    cfg.stream = h->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, grey_step_kernel<STORE, FORCE, MACROS>, C, fin, fout,
+                                             (const int32_t*)h->d_map, (const uint32_t*)h->d_coord,
+                                             (const R*)h->d_ns, (R*)h->d_gstale, (R*)h->d_vprev, (R*)h->d_rho,
+                                             (R*)h->d_v, (const float*)h->d_rref[h->cur], h->d_rref[h->cur ^ 1]);
     h->cur ^= 1;
-    return lbm_cuda_check(h, cudaGetLastError(), "grey_step_kernel launch");
+    return lbm_cuda_check(h, e != cudaSuccess ? e : cudaGetLastError(), "grey_step_kernel launch");
 }
 
 template <int STORE>
