@@ -222,6 +222,29 @@ __device__ __forceinline__ void tp_collide_and_store(typename Codec<STORE>::R* F
     for (int p = 0; p < 9; ++p) cs_out[p * np + n] = cs[p];
 }
 
+// Programmatic dependent launch between the step's launches (A, B, next A):
+// a launch's CTAs may become resident while the previous launch drains; they
+// load their coordinates, then wait for it to complete before touching any
+// state (the wait returns at once for a launch without the attribute).
+__device__ __forceinline__ void tp_pdl_launch_dependents() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+__device__ __forceinline__ void tp_pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename K, typename... Args>
+cudaError_t tp_launch_pdl(K kernel, int grid, int block, cudaStream_t stream, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 // ---------------------------------------------------------------- launch A
 template <int Q, typename R>
 __device__ __forceinline__ void colour_pull_one(const TpConsts<R>& T, const int32_t* __restrict__ map,
@@ -266,6 +289,7 @@ __global__ void __launch_bounds__(256) tp_colour_kernel(const __grid_constant__ 
                                                         R* __restrict__ rr_out, R* __restrict__ rb_out,
                                                         R* __restrict__ psi_out, const int32_t* __restrict__ map,
                                                         const uint32_t* __restrict__ coord) {
+    tp_pdl_launch_dependents();
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= T.sp.n_fluid) return;
     const uint32_t pc = __ldg(coord + n);
@@ -276,6 +300,7 @@ __global__ void __launch_bounds__(256) tp_colour_kernel(const __grid_constant__ 
     const int zm = k == 0 ? nz - 1 : k - 1, zp = k == nz - 1 ? 0 : k + 1;
     const Rows rows = make_rows(nx, ny, i, j, k, ym, yp, zm, zp);
     const bool xwrap = !(i > 0 && i < nx - 1);
+    tp_pdl_wait();  // v, cs of the previous flow launch; psi is rewritten below
     R ar = (R)0, ab = (R)0;
 #define LBM_CP(Q) colour_pull_one<Q, R>(T, map, rows, n, i, xm, xp, xwrap, rr_in, rb_in, v, cs, ar, ab);
     LBM_CP(0) LBM_ALL_DIRS(LBM_CP)
@@ -317,11 +342,13 @@ __global__ void __launch_bounds__(256) tp_flow_kernel(const __grid_constant__ Tp
     using Cd = Codec<STORE>;
     using R = typename Cd::R;
     const SpConsts<R>& C = T.sp;
+    tp_pdl_launch_dependents();
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= C.n_fluid) return;
     const uint32_t pc = __ldg(coord + n);
     const int i = lbm_pi(pc), j = lbm_pj(pc), k = lbm_pk(pc);
     const int64_t np = C.np;
+    tp_pdl_wait();  // rho_r, rho_b, psi of the colour launch; f, v, cs of the previous step
     R F[19];
     gather_node<STORE>(F, fin, map, n, C.nx, C.ny, C.nz, i, j, k, rref_in);
     if (C.any_bc && on_face(i, j, k, C, false)) apply_faces<R, Cd::DEV>(F, i, j, k, n, C, map, v);  // v: previous step
@@ -435,17 +462,18 @@ int tp_steps_t(LbmHandle* h, int32_t nsteps) {
     auto kb = h->force ? tp_flow_kernel<STORE, true> : tp_flow_kernel<STORE, false>;
     for (int32_t it = 0; it < nsteps; ++it) {
         const int c = h->ccur;
-        tp_colour_kernel<R><<<grid, h->block, 0, h->stream>>>(T, (const R*)h->d_rr[c], (const R*)h->d_rb[c],
-                                                              (const R*)h->d_v, (const R*)h->d_cs, (R*)h->d_rr[c ^ 1],
-                                                              (R*)h->d_rb[c ^ 1], (R*)h->d_psi, h->d_map, h->d_coord);
-        int rc = lbm_cuda_check(h, cudaGetLastError(), "tp_colour_kernel launch");
+        cudaError_t e = tp_launch_pdl(tp_colour_kernel<R>, grid, h->block, h->stream, T, (const R*)h->d_rr[c],
+                                      (const R*)h->d_rb[c], (const R*)h->d_v, (const R*)h->d_cs, (R*)h->d_rr[c ^ 1],
+                                      (R*)h->d_rb[c ^ 1], (R*)h->d_psi, (const int32_t*)h->d_map,
+                                      (const uint32_t*)h->d_coord);
+        int rc = lbm_cuda_check(h, e != cudaSuccess ? e : cudaGetLastError(), "tp_colour_kernel launch");
         if (rc) return rc;
         h->ccur ^= 1;
-        kb<<<grid, h->block, 0, h->stream>>>(T, (const Tt*)h->d_f[h->cur], (Tt*)h->d_f[h->cur ^ 1], h->d_map, h->d_coord,
-                                             (R*)h->d_v, (R*)h->d_rho, (const R*)h->d_rr[h->ccur],
-                                             (const R*)h->d_rb[h->ccur], (const R*)h->d_psi, (R*)h->d_cs,
-                                             h->d_rref[h->cur], h->d_rref[h->cur ^ 1]);
-        rc = lbm_cuda_check(h, cudaGetLastError(), "tp_flow_kernel launch");
+        e = tp_launch_pdl(kb, grid, h->block, h->stream, T, (const Tt*)h->d_f[h->cur], (Tt*)h->d_f[h->cur ^ 1],
+                          (const int32_t*)h->d_map, (const uint32_t*)h->d_coord, (R*)h->d_v, (R*)h->d_rho,
+                          (const R*)h->d_rr[h->ccur], (const R*)h->d_rb[h->ccur], (const R*)h->d_psi, (R*)h->d_cs,
+                          (const float*)h->d_rref[h->cur], h->d_rref[h->cur ^ 1]);
+        rc = lbm_cuda_check(h, e != cudaSuccess ? e : cudaGetLastError(), "tp_flow_kernel launch");
         if (rc) return rc;
         h->cur ^= 1;
     }
