@@ -417,7 +417,7 @@ def cavity(steps=1000, log=lambda m: print(m, file=sys.stderr, flush=True)):
             "note": "first launches included (no warm-up): the lattice is L2-resident"}
 
 
-def unet_step(steps=10, warmup=3, n=2, edge=96):
+def unet_step(steps=10, warmup=3, n=2, edge=96, activation="relu"):
     """Warm-start U-Net training step (forward, masked MSE, backward, Adam) on
     n seeded random samples of edge^3 with 16 input channels: ms per step from
     CUDA events, and the convolution work per step (forward, backward-data and
@@ -425,7 +425,7 @@ def unet_step(steps=10, warmup=3, n=2, edge=96):
     import torch
     from taichi_lbm3d_gb300.unet import LAYERS, UNet3D
     torch.manual_seed(0)
-    m = UNet3D(seed=0)
+    m = UNet3D(seed=0, activation=activation)
     x = torch.randn((n, edge, edge, edge, 16), device="cuda").to(torch.bfloat16)
     t = torch.randn((n, edge, edge, edge, 4), device="cuda")
     mk = torch.ones((n, edge, edge, edge), device="cuda", dtype=torch.uint8)
@@ -452,6 +452,7 @@ def unet_step(steps=10, warmup=3, n=2, edge=96):
         vox = n * (edge >> lv) ** 3
         flop += 3 * 2.0 * vox * 27 * cin * cout
     return {"workload": "U-Net training step, %d x %d^3, 16 input channels, random data" % (n, edge),
+            "activation": activation,
             "steps": steps, "ms_per_step": ms, "conv_tflops": flop / (ms * 1e-3) / 1e12,
             "loss_finite": bool(torch.isfinite(loss).all().item())}
 
@@ -589,7 +590,8 @@ def main():
         print(json.dumps({"voxelize": voxelize_bench()}))
         return 0
     if a.unet:
-        print(json.dumps({"unet": unet_step(steps=a.steps or 10)}))
+        print(json.dumps({"unet": unet_step(steps=a.steps or 10),
+                          "unet_gelu": unet_step(steps=a.steps or 10, activation="gelu")}))
         return 0
     if a.grey:
         print(json.dumps({"grey": grey(steps=a.steps or 1000, cpu=not a.no_cpu_baseline)}))

@@ -25,6 +25,13 @@ extern "C" {
  * Any voxel count; cin a multiple of 16 up to 128; cout in {16, 32, 48, 64, 96}. */
 int lbm_nn_conv3d(const void* in, const void* w, const float* bias, const void* mask, void* out, int32_t n, int32_t d,
                   int32_t h, int32_t wd, int32_t cin, int32_t cout, int32_t mode, void* stream);
+/* Same convolution with the activation choice: mode 0 and 1 as above; mode 2:
+ * pre = conv(in, w) + bias, out = gelu(pre) (exact erf form; pre must be given,
+ * same shape as out); mode 3: out = conv(in, w) * gelu'(mask) (mask = the
+ * pre-activation of the layer being back-propagated into; NULL: no factor). */
+int lbm_nn_conv3d_act(const void* in, const void* w, const float* bias, const void* mask, void* out, void* pre,
+                      int32_t n, int32_t d, int32_t h, int32_t wd, int32_t cin, int32_t cout, int32_t mode,
+                      void* stream);
 /* *timed_out = 1 when a tensor-core convolution gave up waiting on its
  * pipeline since the last call (its output is then invalid); clears the flag. */
 int lbm_nn_tc_status(int32_t* timed_out);
@@ -66,6 +73,15 @@ int lbm_nn_head(const void* x, const float* w, const float* b, float* y, int64_t
                 void* stream);
 int lbm_nn_head_bwd(const float* gy, const float* w, const void* x, void* gx, float* dw_db, float* scratch,
                     int64_t nvox, int32_t cin, int32_t cout, void* stream);
+/* The head's backward for either activation of its input x: act 0 (ReLU) as
+ * lbm_nn_head_bwd; act 1 (GELU) gx = gelu'(pre) * gy w with pre the
+ * pre-activation of x. */
+int lbm_nn_head_bwd_act(const float* gy, const float* w, const void* x, const void* pre, void* gx, float* dw_db,
+                        float* scratch, int64_t nvox, int32_t cin, int32_t cout, int32_t act, void* stream);
+/* g *= act'(d) in place over count BF16 elements: act 0 (ReLU) with d the
+ * activation or pre-activation (factor d > 0), act 1 (GELU) with d the
+ * pre-activation. */
+int lbm_nn_act_bwd(void* g, const void* d, int64_t count, int32_t act, void* stream);
 /* Masked MSE: loss = inv_count * sum over mask voxels of (y - t)^2, gy = its
  * gradient; scratch of 256 floats. */
 int lbm_nn_mse(const float* y, const float* t, const uint8_t* mask, float* gy, float* loss, float* scratch,

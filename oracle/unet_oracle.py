@@ -75,13 +75,37 @@ def relu(x):
     return np.maximum(x, 0.0)
 
 
-def forward(P, x):
-    """P: parameter dict (w_<name>, b_<name>, hw, hb) as FP64 arrays; x (D,H,W,16)."""
+def _erf(x):
+    from scipy.special import erf
+    return erf(x)
+
+
+def gelu(x):
+    """Exact GELU, x * Phi(x) = x/2 (1 + erf(x / sqrt 2))."""
+    return 0.5 * x * (1.0 + _erf(x / np.sqrt(2.0)))
+
+
+def gelu_grad(x):
+    """d gelu / dx = Phi(x) + x phi(x)."""
+    return 0.5 * (1.0 + _erf(x / np.sqrt(2.0))) + x * np.exp(-0.5 * x * x) / np.sqrt(2.0 * np.pi)
+
+
+def act_fwd(x, act):
+    return relu(x) if act == "relu" else gelu(x)
+
+
+def act_grad(pre, act):
+    return (pre > 0).astype(np.float64) if act == "relu" else gelu_grad(pre)
+
+
+def forward(P, x, act="relu"):
+    """P: parameter dict (w_<name>, b_<name>, hw, hb) as FP64 arrays; x (D,H,W,16);
+    act: "relu" or "gelu" after every 3x3x3 convolution."""
     a = {"x": x}
 
     def conv(name, src):
         a["pre_" + name] = conv_fwd(src, P["w_" + name], P["b_" + name])
-        a[name] = relu(a["pre_" + name])
+        a[name] = act_fwd(a["pre_" + name], act)
         return a[name]
 
     conv("e1", x)
@@ -102,9 +126,13 @@ def forward(P, x):
     return y, a
 
 
-def loss_and_grads(P, x, target, mask):
+def loss_and_grads(P, x, target, mask, act="relu"):
     """Masked MSE (mean over mask voxels x 4 channels) and its gradient w.r.t. every parameter."""
-    y, a = forward(P, x)
+    y, a = forward(P, x, act)
+
+    def dact(name):
+        return act_grad(a["pre_" + name], act)
+
     m = mask[..., None].astype(np.float64)
     count = float(mask.sum()) * y.shape[-1]
     d = (y - target) * m
@@ -113,27 +141,27 @@ def loss_and_grads(P, x, target, mask):
     G = {}
     G["hw"] = gy.reshape(-1, gy.shape[-1]).T @ a["d1b"].reshape(-1, 16)
     G["hb"] = gy.reshape(-1, gy.shape[-1]).sum(axis=0)
-    g = (gy @ P["hw"]) * (a["pre_d1b"] > 0)
+    g = (gy @ P["hw"]) * dact("d1b")
 
     def back(name, src, g):
         dx, G["w_" + name], G["b_" + name] = conv_bwd(src, P["w_" + name], g)
         return dx
 
-    g = back("d1b", a["d1"], g) * (a["pre_d1"] > 0)
+    g = back("d1b", a["d1"], g) * dact("d1")
     g_c1 = back("d1", a["c1"], g)
-    g_d2b = up_bwd(g_c1[..., :32]) * (a["pre_d2b"] > 0)
+    g_d2b = up_bwd(g_c1[..., :32]) * dact("d2b")
     g_e1b_skip = g_c1[..., 32:]
-    g = back("d2b", a["d2"], g_d2b) * (a["pre_d2"] > 0)
+    g = back("d2b", a["d2"], g_d2b) * dact("d2")
     g_c2 = back("d2", a["c2"], g)
-    g_b1b = up_bwd(g_c2[..., :64]) * (a["pre_b1b"] > 0)
+    g_b1b = up_bwd(g_c2[..., :64]) * dact("b1b")
     g_e2b_skip = g_c2[..., 64:]
-    g = back("b1b", a["b1"], g_b1b) * (a["pre_b1"] > 0)
+    g = back("b1b", a["b1"], g_b1b) * dact("b1")
     g_p2 = back("b1", a["p2"], g)
-    g_e2b = (pool_bwd(g_p2, a["arg2"], a["e2b"].shape) + g_e2b_skip) * (a["pre_e2b"] > 0)
-    g = back("e2b", a["e2"], g_e2b) * (a["pre_e2"] > 0)
+    g_e2b = (pool_bwd(g_p2, a["arg2"], a["e2b"].shape) + g_e2b_skip) * dact("e2b")
+    g = back("e2b", a["e2"], g_e2b) * dact("e2")
     g_p1 = back("e2", a["p1"], g)
-    g_e1b = (pool_bwd(g_p1, a["arg1"], a["e1b"].shape) + g_e1b_skip) * (a["pre_e1b"] > 0)
-    g = back("e1b", a["e1"], g_e1b) * (a["pre_e1"] > 0)
+    g_e1b = (pool_bwd(g_p1, a["arg1"], a["e1b"].shape) + g_e1b_skip) * dact("e1b")
+    g = back("e1b", a["e1"], g_e1b) * dact("e1")
     back("e1", x, g)
     return loss, G, y
 

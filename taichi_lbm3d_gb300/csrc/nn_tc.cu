@@ -26,6 +26,7 @@
 
 #include "../../include/lbm_nn.h"
 #include "lbm_internal.h"
+#include "nn_act.cuh"
 
 namespace {
 typedef __nv_bfloat16 bf16;
@@ -110,11 +111,15 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float* v) {
 // Byte offset of (row, 8-element chunk h) of a K = 16 step in the canonical layout.
 __device__ __forceinline__ uint32_t canon(int row, int h) { return (uint32_t)((row >> 3) * 256 + h * 128 + (row & 7) * 16); }
 
+// MODE 0: out = relu(conv + bias); 1: out = conv * (mask > 0) (mask may be
+// NULL); 2: pre = conv + bias, out = gelu(pre); 3: out = conv * gelu'(mask)
+// (mask = the pre-activation; NULL: no factor).
 template <int COUT, int MODE>
 __global__ void __launch_bounds__(TC_THREADS) conv3d_tc_kernel(const bf16* __restrict__ in, const bf16* __restrict__ w,
                                                               const float* __restrict__ bias,
                                                               const bf16* __restrict__ mask, bf16* __restrict__ out,
-                                                              int N, int D, int H, int W, int cin) {
+                                                              bf16* __restrict__ pre, int N, int D, int H, int W,
+                                                              int cin) {
     constexpr uint32_t NCOL = COUT <= 32 ? 32 : (COUT <= 64 ? 64 : 128);
     constexpr uint32_t IDESC = mma_idesc(TC_M, COUT);
     extern __shared__ __align__(1024) unsigned char smem[];
@@ -240,19 +245,31 @@ __global__ void __launch_bounds__(TC_THREADS) conv3d_tc_kernel(const bf16* __res
             tc_ld16(tw + (uint32_t)c0, acc);
             if (live) {
                 __align__(16) bf16 o[16];
+                __align__(16) bf16 pa[16];
 #pragma unroll
                 for (int q = 0; q < 16; ++q) {
                     float r = acc[q];
                     if constexpr (MODE == 0) {
                         r = fmaxf(r + (bias ? bias[c0 + q] : 0.f), 0.f);
-                    } else {
+                    } else if constexpr (MODE == 1) {
                         if (mask && !(__bfloat162float(mask[v * COUT + c0 + q]) > 0.f)) r = 0.f;
+                    } else if constexpr (MODE == 2) {
+                        r = r + (bias ? bias[c0 + q] : 0.f);
+                        pa[q] = __float2bfloat16_rn(r);
+                        r = nn_gelu(r);
+                    } else {
+                        if (mask) r = r * nn_gelu_grad(__bfloat162float(mask[v * COUT + c0 + q]));
                     }
                     o[q] = __float2bfloat16_rn(r);
                 }
                 uint4* dst = reinterpret_cast<uint4*>(out + v * COUT + c0);
                 dst[0] = reinterpret_cast<const uint4*>(o)[0];
                 dst[1] = reinterpret_cast<const uint4*>(o)[1];
+                if constexpr (MODE == 2) {
+                    uint4* dp = reinterpret_cast<uint4*>(pre + v * COUT + c0);
+                    dp[0] = reinterpret_cast<const uint4*>(pa)[0];
+                    dp[1] = reinterpret_cast<const uint4*>(pa)[1];
+                }
             }
         }
     } else if (tid == 0) {
@@ -265,15 +282,15 @@ __global__ void __launch_bounds__(TC_THREADS) conv3d_tc_kernel(const bf16* __res
 }
 
 template <int COUT, int MODE>
-int launch_tc(const bf16* in, const bf16* w, const float* bias, const bf16* mask, bf16* out, int n, int d, int h,
-              int wd, int cin, cudaStream_t s) {
+int launch_tc(const bf16* in, const bf16* w, const float* bias, const bf16* mask, bf16* out, bf16* pre, int n, int d,
+              int h, int wd, int cin, cudaStream_t s) {
     const size_t smem = (size_t)TC_STAGES * (4096 + (size_t)COUT * 32);
     auto k = conv3d_tc_kernel<COUT, MODE>;
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return lbm_set_err(nullptr, LBM_ECUDA, "lbm_nn_conv3d: shared memory attribute");
     const int64_t nvox = (int64_t)n * d * h * wd;
     const int grid = (int)((nvox + TC_M - 1) / TC_M);
-    k<<<grid, TC_THREADS, smem, s>>>(in, w, bias, mask, out, n, d, h, wd, cin);
+    k<<<grid, TC_THREADS, smem, s>>>(in, w, bias, mask, out, pre, n, d, h, wd, cin);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return lbm_set_err(nullptr, LBM_ECUDA, std::string("conv3d_tc_kernel: ") + cudaGetErrorString(e));
     return LBM_OK;
@@ -564,26 +581,39 @@ __global__ void __launch_bounds__(TC_THREADS) conv3d_wgrad_tc_kernel(const bf16*
 
 extern "C" {
 
-int lbm_nn_conv3d(const void* in, const void* w, const float* bias, const void* mask, void* out, int32_t n, int32_t d,
-                  int32_t h, int32_t wd, int32_t cin, int32_t cout, int32_t mode, void* stream) {
+int lbm_nn_conv3d_act(const void* in, const void* w, const float* bias, const void* mask, void* out, void* pre,
+                      int32_t n, int32_t d, int32_t h, int32_t wd, int32_t cin, int32_t cout, int32_t mode,
+                      void* stream) {
     const int64_t nvox = (int64_t)n * d * h * wd;
-    if (!in || !w || !out || nvox <= 0 || cin % 16 || cin <= 0 || cin > 128 || (mode != 0 && mode != 1))
-        return lbm_set_err(nullptr, LBM_EINVAL, "lbm_nn_conv3d: cin must be a multiple of 16 in [16, 128]; mode 0 or 1");
+    if (!in || !w || !out || nvox <= 0 || cin % 16 || cin <= 0 || cin > 128 || mode < 0 || mode > 3)
+        return lbm_set_err(nullptr, LBM_EINVAL, "lbm_nn_conv3d: cin must be a multiple of 16 in [16, 128]; mode 0..3");
+    if (mode == 2 && !pre) return lbm_set_err(nullptr, LBM_EINVAL, "lbm_nn_conv3d_act: mode 2 needs pre");
     cudaStream_t s = (cudaStream_t)stream;
     const bf16* I = (const bf16*)in;
     const bf16* Wt = (const bf16*)w;
     const bf16* M = (const bf16*)mask;
     bf16* O = (bf16*)out;
-#define LBM_TC(C)                                                                               \
-    case C:                                                                                     \
-        return mode == 0 ? launch_tc<C, 0>(I, Wt, bias, M, O, n, d, h, wd, cin, s)              \
-                         : launch_tc<C, 1>(I, Wt, bias, M, O, n, d, h, wd, cin, s);
+    bf16* P = (bf16*)pre;
+#define LBM_TC(C)                                                                  \
+    case C:                                                                        \
+        switch (mode) {                                                            \
+        case 0: return launch_tc<C, 0>(I, Wt, bias, M, O, P, n, d, h, wd, cin, s); \
+        case 1: return launch_tc<C, 1>(I, Wt, bias, M, O, P, n, d, h, wd, cin, s); \
+        case 2: return launch_tc<C, 2>(I, Wt, bias, M, O, P, n, d, h, wd, cin, s); \
+        default: return launch_tc<C, 3>(I, Wt, bias, M, O, P, n, d, h, wd, cin, s); \
+        }
     switch (cout) {
         LBM_TC(16) LBM_TC(32) LBM_TC(48) LBM_TC(64) LBM_TC(96)
     default:
         return lbm_set_err(nullptr, LBM_EINVAL, "lbm_nn_conv3d: cout must be 16, 32, 48, 64 or 96");
     }
 #undef LBM_TC
+}
+
+int lbm_nn_conv3d(const void* in, const void* w, const float* bias, const void* mask, void* out, int32_t n, int32_t d,
+                  int32_t h, int32_t wd, int32_t cin, int32_t cout, int32_t mode, void* stream) {
+    if (mode != 0 && mode != 1) return lbm_set_err(nullptr, LBM_EINVAL, "lbm_nn_conv3d: mode 0 or 1");
+    return lbm_nn_conv3d_act(in, w, bias, mask, out, nullptr, n, d, h, wd, cin, cout, mode, stream);
 }
 
 // Runs the timeout self-test (about 1e6 cycles of waiting on a barrier nothing

@@ -14,6 +14,7 @@
 
 #include "../../include/lbm_nn.h"
 #include "lbm_internal.h"
+#include "nn_act.cuh"
 
 // tensor-core weight gradient (nn_tc.cu)
 int nn_wgrad_tc_launch(const void* in, const void* g, float* part, float* dbpart, int n, int d, int h, int w, int cin,
@@ -177,17 +178,25 @@ __global__ void head_fwd_kernel(const bf16* __restrict__ x, const float* __restr
     }
 }
 
-// gx[v][c] = (x[v][c] > 0) * sum_o gy[v][o] w[o][c]
+// gx[v][c] = act'(d[v][c]) * sum_o gy[v][o] w[o][c]; d = the head's input x
+// (ReLU) or its pre-activation (GELU)
 __global__ void head_bwd_data_kernel(const float* __restrict__ gy, const float* __restrict__ w,
-                                     const bf16* __restrict__ x, bf16* __restrict__ gx, int64_t nvox, int cin,
-                                     int cout) {
+                                     const bf16* __restrict__ d, bf16* __restrict__ gx, int64_t nvox, int cin,
+                                     int cout, int act) {
     const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= nvox) return;
     for (int c = 0; c < cin; ++c) {
         float s = 0.f;
         for (int o = 0; o < cout; ++o) s = fmaf(gy[v * cout + o], w[o * cin + c], s);
-        gx[v * cin + c] = __float2bfloat16_rn(__bfloat162float(x[v * cin + c]) > 0.f ? s : 0.f);
+        gx[v * cin + c] = __float2bfloat16_rn(s * nn_act_grad(act, __bfloat162float(d[v * cin + c])));
     }
+}
+
+// g[e] *= act'(d[e]) in place
+__global__ void act_bwd_kernel(bf16* __restrict__ g, const bf16* __restrict__ d, int64_t count, int act) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= count) return;
+    g[e] = __float2bfloat16_rn(__bfloat162float(g[e]) * nn_act_grad(act, __bfloat162float(d[e])));
 }
 
 // Head weight/bias gradient partials per block: part[block][o*cin + c], part[block][cout*cin + o].
@@ -348,8 +357,17 @@ int lbm_nn_head(const void* x, const float* w, const float* b, float* y, int64_t
 
 int lbm_nn_head_bwd(const float* gy, const float* w, const void* x, void* gx, float* dw_db, float* scratch,
                     int64_t nvox, int32_t cin, int32_t cout, void* stream) {
+    return lbm_nn_head_bwd_act(gy, w, x, nullptr, gx, dw_db, scratch, nvox, cin, cout, LBM_NN_ACT_RELU, stream);
+}
+
+int lbm_nn_head_bwd_act(const float* gy, const float* w, const void* x, const void* pre, void* gx, float* dw_db,
+                        float* scratch, int64_t nvox, int32_t cin, int32_t cout, int32_t act, void* stream) {
+    if (act != LBM_NN_ACT_RELU && act != LBM_NN_ACT_GELU)
+        return lbm_set_err(nullptr, LBM_EINVAL, "lbm_nn_head_bwd_act: act 0 (ReLU) or 1 (GELU)");
+    if (act == LBM_NN_ACT_GELU && !pre) return lbm_set_err(nullptr, LBM_EINVAL, "lbm_nn_head_bwd_act: GELU needs pre");
     cudaStream_t s = (cudaStream_t)stream;
-    head_bwd_data_kernel<<<blocks(nvox, 128), 128, 0, s>>>(gy, w, (const bf16*)x, (bf16*)gx, nvox, cin, cout);
+    const bf16* d = (const bf16*)(act == LBM_NN_ACT_GELU ? pre : x);
+    head_bwd_data_kernel<<<blocks(nvox, 128), 128, 0, s>>>(gy, w, d, (bf16*)gx, nvox, cin, cout, act);
     int rc = check("head_bwd_data_kernel");
     if (rc) return rc;
     const int nb = 256, nout = cout * cin + cout;
@@ -358,6 +376,15 @@ int lbm_nn_head_bwd(const float* gy, const float* w, const void* x, void* gx, fl
     if (rc) return rc;
     sum_partials_kernel<<<blocks(nout), 256, 0, s>>>(scratch, dw_db, nb, nout);
     return check("sum_partials_kernel");
+}
+
+int lbm_nn_act_bwd(void* g, const void* d, int64_t count, int32_t act, void* stream) {
+    if (act != LBM_NN_ACT_RELU && act != LBM_NN_ACT_GELU)
+        return lbm_set_err(nullptr, LBM_EINVAL, "lbm_nn_act_bwd: act 0 (ReLU) or 1 (GELU)");
+    if (!g || !d || count < 0) return lbm_set_err(nullptr, LBM_EINVAL, "lbm_nn_act_bwd: null pointer or count < 0");
+    if (count == 0) return LBM_OK;
+    act_bwd_kernel<<<blocks(count, 256), 256, 0, (cudaStream_t)stream>>>((bf16*)g, (const bf16*)d, count, act);
+    return check("act_bwd_kernel");
 }
 
 int lbm_nn_mse(const float* y, const float* t, const uint8_t* mask, float* gy, float* loss, float* scratch,

@@ -6,8 +6,9 @@ f = feq(rho, v) instead of rest (``LB3D_Solver_Single_Phase.init_simulation(rho,
 and runs to the same convergence criterion, so it judges the prediction and
 falls back to plain iteration where the prediction is poor.
 
-Architecture (3 levels, channels 16/32/64): two 3x3x3 conv + ReLU per level,
-2x max-pool down, 2x nearest upsample + skip concat up, 1x1 head to 4 outputs.
+Architecture (3 levels, channels 16/32/64): two 3x3x3 conv + activation per
+level (ReLU, or the exact GELU with ``activation="gelu"``), 2x max-pool down, 2x
+nearest upsample + skip concat up, 1x1 head to 4 outputs.
 Forward and backward run entirely in the project's CUDA kernels
 (csrc/nn_unet.cu, C ABI include/lbm_nn.h); torch provides device memory and the
 stream only.  Weights are kept in FP32 (Adam master copy) and used in BF16.
@@ -30,6 +31,9 @@ _L = ctypes.c_int64
 _F = ctypes.c_float
 _SIGS = {
     "lbm_nn_conv3d": ([_P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _I, _P], ctypes.c_int),
+    "lbm_nn_conv3d_act": ([_P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _I, _P], ctypes.c_int),
+    "lbm_nn_head_bwd_act": ([_P, _P, _P, _P, _P, _P, _P, _L, _I, _I, _I, _P], ctypes.c_int),
+    "lbm_nn_act_bwd": ([_P, _P, _L, _I, _P], ctypes.c_int),
     "lbm_nn_tc_status": ([_P], ctypes.c_int),
     "lbm_nn_tc_timeout_selftest": ([_P], ctypes.c_int),
     "lbm_nn_flip_transpose": ([_P, _P, _I, _I, _P], ctypes.c_int),
@@ -68,10 +72,16 @@ def _ck(rc):
         raise _native.LbmError(rc, _native.last_error())
 
 
+ACTIVATIONS = {"relu": 0, "gelu": 1}
+
+
 class UNet3D:
-    def __init__(self, seed=0):
+    def __init__(self, seed=0, activation="relu"):
         import torch
+        if activation not in ACTIVATIONS:
+            raise ValueError("activation must be 'relu' or 'gelu'")
         self.torch = torch
+        self.activation = activation
         g = torch.Generator().manual_seed(seed)
         self.w, self.b, self.w16, self.wt16 = {}, {}, {}, {}
         self.params = []          # (name, master, grad, m, v, bf16 copy or None)
@@ -116,6 +126,7 @@ class UNet3D:
         d["hw"] = self.hw.cpu().numpy()
         d["hb"] = self.hb.cpu().numpy()
         d["scales"] = self.scales
+        d["activation"] = np.array(ACTIVATIONS[self.activation], np.int32)
         return d
 
     def load_state_dict(self, d):
@@ -125,6 +136,9 @@ class UNet3D:
         self.hw.copy_(self.torch.from_numpy(np.asarray(d["hw"])))
         self.hb.copy_(self.torch.from_numpy(np.asarray(d["hb"])))
         self.scales = np.asarray(d["scales"], np.float32)
+        if "activation" in d:
+            code = int(np.asarray(d["activation"]))
+            self.activation = next(k for k, v in ACTIVATIONS.items() if v == code)
         self.refresh()
 
     # ----------------------------------------------------------- forward
@@ -147,12 +161,17 @@ class UNet3D:
         dims = {0: (N, D, H, W), 1: (N, D // 2, H // 2, W // 2), 2: (N, D // 4, H // 4, W // 4)}
         a = {"x": x16}
 
+        gelu = self.activation == "gelu"
+
         def conv(name, src):
             _, cin, cout, lv = next(l for l in LAYERS if l[0] == name)
             out = self._buf("a_" + name, dims[lv] + (cout,), t.bfloat16)
-            _ck(L.lbm_nn_conv3d(_p(src), _p(self.w16[name]), _p(self.b[name]), None, _p(out), *dims[lv], cin, cout,
-                                0, s))
+            pre = self._buf("pre_" + name, dims[lv] + (cout,), t.bfloat16) if gelu else None
+            _ck(L.lbm_nn_conv3d_act(_p(src), _p(self.w16[name]), _p(self.b[name]), None, _p(out), _p(pre),
+                                    *dims[lv], cin, cout, 2 if gelu else 0, s))
             a[name] = out
+            if gelu:
+                a["pre_" + name] = pre
             return out
 
         def pool(name, src, lv, c):
@@ -199,6 +218,19 @@ class UNet3D:
         s = self._stream()
         a, dims = self._a, self._dims
         nv0 = int(np.prod(dims[0]))
+        gelu = self.activation == "gelu"
+        act = ACTIVATIONS[self.activation]
+
+        def dmask(name):
+            """What the masked kernels multiply by: ReLU -> the activation (factor > 0),
+            GELU -> the pre-activation (factor gelu')."""
+            return a["pre_" + name] if gelu else a[name]
+
+        def act_bwd(g, name):
+            """GELU only: the pooling/upsampling backward kernels know the ReLU mask
+            alone, so their GELU factor is applied by a separate pass."""
+            if gelu:
+                _ck(L.lbm_nn_act_bwd(_p(g), _p(a["pre_" + name]), g.numel(), act, s))
 
         def g_buf(name, lv, c):
             return self._buf("g_" + name, dims[lv] + (c,), t.bfloat16)
@@ -216,27 +248,29 @@ class UNet3D:
         def bwd_data(name, g, mask, out_key):
             _, cin, cout, lv = next(l for l in LAYERS if l[0] == name)
             out = g_buf(out_key, lv, cin)
-            _ck(L.lbm_nn_conv3d(_p(g), _p(self.wt16[name]), None, _p(mask), _p(out), *dims[lv], cout, cin, 1, s))
+            _ck(L.lbm_nn_conv3d_act(_p(g), _p(self.wt16[name]), None, _p(mask), _p(out), None, *dims[lv], cout, cin,
+                                    3 if gelu else 1, s))
             return out
 
         # head
         g_d1b = g_buf("d1b", 0, 16)
         hs = self._buf("head_scratch", (256 * (OUT * 16 + OUT),), t.float32)
-        _ck(L.lbm_nn_head_bwd(_p(gy), _p(self.hw), _p(a["d1b"]), _p(g_d1b), _p(self.ghw_hb), _p(hs), nv0, 16, OUT,
-                              s))
+        _ck(L.lbm_nn_head_bwd_act(_p(gy), _p(self.hw), _p(a["d1b"]), _p(a.get("pre_d1b")), _p(g_d1b),
+                                  _p(self.ghw_hb), _p(hs), nv0, 16, OUT, act, s))
         # level 0 decoder
         wgrad("d1b", a["d1"], g_d1b)
-        g_d1 = bwd_data("d1b", g_d1b, a["d1"], "d1")
+        g_d1 = bwd_data("d1b", g_d1b, dmask("d1"), "d1")
         wgrad("d1", a["c1"], g_d1)
         g_c1 = bwd_data("d1", g_d1, None, "c1")
         g_u1 = g_buf("u1", 0, 32)
         g_e1b = g_buf("e1b", 0, 16)
         _ck(L.lbm_nn_split(_p(g_c1), 32, 16, _p(g_u1), _p(g_e1b), None, 0, nv0, s))
         g_d2b = g_buf("d2b", 1, 32)
-        _ck(L.lbm_nn_upsample2_bwd(_p(g_u1), _p(g_d2b), _p(a["d2b"]), *dims[1], 32, s))
+        _ck(L.lbm_nn_upsample2_bwd(_p(g_u1), _p(g_d2b), None if gelu else _p(a["d2b"]), *dims[1], 32, s))
+        act_bwd(g_d2b, "d2b")
         # level 1 decoder
         wgrad("d2b", a["d2"], g_d2b)
-        g_d2 = bwd_data("d2b", g_d2b, a["d2"], "d2")
+        g_d2 = bwd_data("d2b", g_d2b, dmask("d2"), "d2")
         wgrad("d2", a["c2"], g_d2)
         g_c2 = bwd_data("d2", g_d2, None, "c2")
         nv1 = int(np.prod(dims[1]))
@@ -244,22 +278,27 @@ class UNet3D:
         g_e2b = g_buf("e2b", 1, 32)
         _ck(L.lbm_nn_split(_p(g_c2), 64, 32, _p(g_u2), _p(g_e2b), None, 0, nv1, s))
         g_b1b = g_buf("b1b", 2, 64)
-        _ck(L.lbm_nn_upsample2_bwd(_p(g_u2), _p(g_b1b), _p(a["b1b"]), *dims[2], 64, s))
+        _ck(L.lbm_nn_upsample2_bwd(_p(g_u2), _p(g_b1b), None if gelu else _p(a["b1b"]), *dims[2], 64, s))
+        act_bwd(g_b1b, "b1b")
         # bottleneck
         wgrad("b1b", a["b1"], g_b1b)
-        g_b1 = bwd_data("b1b", g_b1b, a["b1"], "b1")
+        g_b1 = bwd_data("b1b", g_b1b, dmask("b1"), "b1")
         wgrad("b1", a["p2"], g_b1)
         g_p2 = bwd_data("b1", g_b1, None, "p2")
-        _ck(L.lbm_nn_pool2_bwd(_p(g_p2), _p(a["arg_p2"]), _p(g_e2b), _p(a["e2b"]), *dims[1], 32, 1, s))
+        _ck(L.lbm_nn_pool2_bwd(_p(g_p2), _p(a["arg_p2"]), _p(g_e2b), None if gelu else _p(a["e2b"]), *dims[1], 32,
+                               1, s))
+        act_bwd(g_e2b, "e2b")
         # level 1 encoder
         wgrad("e2b", a["e2"], g_e2b)
-        g_e2 = bwd_data("e2b", g_e2b, a["e2"], "e2")
+        g_e2 = bwd_data("e2b", g_e2b, dmask("e2"), "e2")
         wgrad("e2", a["p1"], g_e2)
         g_p1 = bwd_data("e2", g_e2, None, "p1")
-        _ck(L.lbm_nn_pool2_bwd(_p(g_p1), _p(a["arg_p1"]), _p(g_e1b), _p(a["e1b"]), *dims[0], 16, 1, s))
+        _ck(L.lbm_nn_pool2_bwd(_p(g_p1), _p(a["arg_p1"]), _p(g_e1b), None if gelu else _p(a["e1b"]), *dims[0], 16,
+                               1, s))
+        act_bwd(g_e1b, "e1b")
         # level 0 encoder
         wgrad("e1b", a["e1"], g_e1b)
-        g_e1 = bwd_data("e1b", g_e1b, a["e1"], "e1")
+        g_e1 = bwd_data("e1b", g_e1b, dmask("e1"), "e1")
         wgrad("e1", a["x"], g_e1)
 
     def grads(self):

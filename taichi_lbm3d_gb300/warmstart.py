@@ -231,6 +231,8 @@ def main(argv=None):
     ap.add_argument("--eval-edge", type=int, default=192)
     ap.add_argument("--eval-seed0", type=int, default=20000)
     ap.add_argument("--fp64-subset", type=int, default=4)
+    ap.add_argument("--activation", default="relu", choices=["relu", "gelu"],
+                    help="activation after every 3x3x3 convolution of the network")
     ap.add_argument("--weights", default=None, help="load trained weights instead of training")
     ap.add_argument("--out", default="warmstart_weights.npz")
     ap.add_argument("--report", default="warmstart_report.json")
@@ -244,8 +246,9 @@ def main(argv=None):
     eval_in = make_inputs(range(a.eval_seed0, a.eval_seed0 + a.eval_n), a.eval_edge)
     log("inputs ready in %.1f s" % (time.perf_counter() - t0))
     from .unet import UNet3D
-    model = UNet3D(seed=0)
-    report = {"n_params": model.n_params(), "train_n": a.train_n, "edge": a.edge, "eval_n": a.eval_n,
+    model = UNet3D(seed=0, activation=a.activation)
+    report = {"n_params": model.n_params(), "activation": a.activation, "train_n": a.train_n, "edge": a.edge,
+              "eval_n": a.eval_n,
               "eval_edge": a.eval_edge}
     if a.weights:
         model.load_state_dict(dict(np.load(a.weights)))

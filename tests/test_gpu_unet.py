@@ -33,9 +33,9 @@ def case(seed=3, n=16):
     return P, x, t, mask
 
 
-def gpu_model(P):
+def gpu_model(P, act="relu"):
     from taichi_lbm3d_gb300.unet import UNet3D
-    m = UNet3D(seed=0)
+    m = UNet3D(seed=0, activation=act)
     d = {k: np.asarray(v, np.float32) for k, v in P.items()}
     d["scales"] = np.ones(4, np.float32)
     m.load_state_dict(d)
@@ -54,10 +54,12 @@ def rel(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
 
 
-def test_forward_and_gradients_match_cpu_oracle():
+@pytest.mark.parametrize("act", ["relu", "gelu"])
+def test_forward_and_gradients_match_cpu_oracle(act):
+    pytest.importorskip("scipy")
     P, x, t, mask = case()
-    loss_ref, G_ref, y_ref = U.loss_and_grads(P, x, t, mask)
-    m = gpu_model(P)
+    loss_ref, G_ref, y_ref = U.loss_and_grads(P, x, t, mask, act)
+    m = gpu_model(P, act)
     xg, tg, mg = to_gpu(x, t, mask)
     y = m.forward(xg)
     loss, gy = m.loss(y, tg, mg, float(mask.sum()) * 4)
@@ -74,15 +76,16 @@ def test_forward_and_gradients_match_cpu_oracle():
         e = rel(g, ref)
         cos = float((g * ref).sum() / (np.linalg.norm(g) * np.linalg.norm(ref) + 1e-30))
         worst.append((e, cos, k))
-    print("forward %.3e loss %.3e worst grads %s" % (e_y, e_l, sorted(worst)[-3:]))
+    print("%s forward %.3e loss %.3e worst grads %s" % (act, e_y, e_l, sorted(worst)[-3:]))
     assert e_y < Y_TOL and e_l < Y_TOL
     for e, cos, k in worst:
         assert e < G_TOL and cos > G_COS, (k, e, cos)
 
 
-def test_training_reduces_loss():
+@pytest.mark.parametrize("act", ["relu", "gelu"])
+def test_training_reduces_loss(act):
     P, x, t, mask = case(seed=4)
-    m = gpu_model(P)
+    m = gpu_model(P, act)
     xg, tg, mg = to_gpu(x, 0.1 * t, mask)
     losses = []
     for _ in range(40):

@@ -1,6 +1,7 @@
 """The FP64 CPU oracle of the warm-start network: its hand-written backward
 matches central finite differences (so it can check the GPU kernels)."""
 import numpy as np
+import pytest
 
 from oracle import unet_oracle as U
 
@@ -16,9 +17,11 @@ def small_case(seed=0, n=8):
     return P, x, t, mask
 
 
-def test_backward_matches_finite_differences():
+@pytest.mark.parametrize("act", ["relu", "gelu"])
+def test_backward_matches_finite_differences(act):
+    pytest.importorskip("scipy")
     P, x, t, mask = small_case()
-    loss, G, _ = U.loss_and_grads(P, x, t, mask)
+    loss, G, _ = U.loss_and_grads(P, x, t, mask, act)
     rng = np.random.default_rng(1)
     eps = 1e-6
     for key in ["w_e1", "w_e2b", "w_b1b", "b_d2", "w_d1", "b_d1b", "hw", "hb"]:
@@ -29,9 +32,9 @@ def test_backward_matches_finite_differences():
                 idx = idx[:2] + (int(idx[2]) % 2,)
             old = arr[idx]
             arr[idx] = old + eps
-            lp = U.loss_and_grads(P, x, t, mask)[0]
+            lp = U.loss_and_grads(P, x, t, mask, act)[0]
             arr[idx] = old - eps
-            lm = U.loss_and_grads(P, x, t, mask)[0]
+            lm = U.loss_and_grads(P, x, t, mask, act)[0]
             arr[idx] = old
             fd = (lp - lm) / (2 * eps)
-            assert abs(fd - G[key][idx]) <= 1e-6 * max(1.0, abs(fd)), (key, idx, fd, G[key][idx])
+            assert abs(fd - G[key][idx]) <= 1e-6 * max(1.0, abs(fd)), (act, key, idx, fd, G[key][idx])
