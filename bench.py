@@ -690,6 +690,9 @@ def main():
                      "traffic": (tpn * nf) if tpn else None,
                      "algorithmic_bytes_per_node": BYTES_PER_NODE["f32"]},
         "checks": {"mass": st.mass, "n_nonfinite": st.n_nonfinite},
+        # all lattice cells (solid included) per second: the unit of the
+        # reference's own MLUPS figures, which count every cell of the box
+        "total_cell_mlups": mlups * float(solid.size) / nf,
     }
     if rank == 0:
         if not a.no_variants:
