@@ -474,8 +474,9 @@ def grey_field(shape=SHAPE):
 def grey(steps=1000, cpu=True, cpu_seconds=20.0, log=lambda m: print(m, file=sys.stderr, flush=True)):
     """Grey-scale (partial bounce-back) step on the grey 256^3 field: body
     force fx = 1e-6, periodic, niu 0.1 (script conventions).  MLUPS with CUDA
-    events on the library's stream, FP32 and FP16; the CPU oracle's grey sweeps
-    on a bounded sample of the same lattice."""
+    events on the library's stream for FP32 reference arithmetic, FP32
+    deviation form and FP16; the CPU oracle's grey sweeps on a bounded sample
+    of the same lattice."""
     import torch
     from taichi_lbm3d_gb300 import LB3D_Solver_Grey_Scale
     ns = grey_field()
@@ -484,7 +485,7 @@ def grey(steps=1000, cpu=True, cpu_seconds=20.0, log=lambda m: print(m, file=sys
                        "within 1.5 cells of them, fx 1e-6, periodic, niu 0.1",
            "n_fluid": nf, "n_grey": int(((ns > 0) & (ns < 1)).sum()), "steps": steps}
     peak, kind = measured_peak()
-    for sto in ("f32", "f16"):
+    for sto in ("f32", "f32dev", "f16"):
         lb = LB3D_Solver_Grey_Scale(*SHAPE, storage=sto)
         lb.fx = 1e-6
         lb.ns.from_numpy(ns)
@@ -502,7 +503,7 @@ def grey(steps=1000, cpu=True, cpu_seconds=20.0, log=lambda m: print(m, file=sys
         secs = e0.elapsed_time(e1) / 1e3
         mlups = nf * steps / secs / 1e6
         # algorithmic bytes per node: populations in + out, plus the node's ns
-        bpn = {"f32": 156, "f16": 80}[sto]
+        bpn = {"f32": 156, "f32dev": 156, "f16": 80}[sto]
         out["mlups_" + sto] = mlups
         out["gbs_algorithmic_" + sto] = bpn * mlups / 1e3
         out["roofline_frac_" + sto] = bpn * mlups / 1e3 / peak
