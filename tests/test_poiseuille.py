@@ -1,0 +1,83 @@
+"""Known answer: body-force driven channel flow between two solid walls
+(halfway bounce-back) reaches the analytic parabola
+
+    u(y) = F_eff / (2 nu_eff) (y - 1/2) (ny - 3/2 - y),  fluid rows y = 1 .. ny-2,
+
+with nu_eff and F_eff of the chosen conventions: viscosity "standard"
+(tau = 3 nu + 1/2) nu_eff = nu, "class" (tau = nu/3 + 1/2, SP:127) nu/9; Guo
+"standard" F_eff = F, "class" (SP:236) F/9, "script" (TP:246) F/3.  The MRT
+rates satisfy (1/s_v - 1/2)(1/s_q - 1/2) = 3/16 (s_q = 8(2 - s_v)/(8 - s_v),
+SP:131), for which halfway bounce-back gives the parabola exactly, so the
+consistent "standard" pair matches to round-off.  The class and script forms
+shift the velocity by F/2 while injecting F_eff, which leaves a small offset."""
+import numpy as np
+import pytest
+
+H = 16
+NY = H + 2
+SHAPE = (4, NY, 4)
+NIU = 0.1
+F = 1e-6
+# (viscosity convention, Guo convention) -> (nu_eff factor, F_eff factor, FP64 tolerance)
+CONVENTIONS = {"standard": (1, 2, 1.0, 1.0, 1e-8), "class": (0, 0, 1 / 9, 1 / 9, 5e-3),
+               "script": (1, 1, 1.0, 1 / 3, 5e-3)}
+
+
+def channel():
+    solid = np.zeros(SHAPE, np.int8)
+    solid[:, 0, :] = 1
+    solid[:, -1, :] = 1
+    return solid
+
+
+def analytic(nu_f, f_f):
+    y = np.arange(1, NY - 1, dtype=np.float64)
+    return (F * f_f) / (2 * NIU * nu_f) * (y - 0.5) * (NY - 1.5 - y)
+
+
+def rel_err(vx, u):
+    return float(np.abs(vx - u).max() / np.abs(u).max())
+
+
+@pytest.mark.parametrize("conv", list(CONVENTIONS))
+def test_oracle_channel_flow_matches_parabola(conv):
+    from oracle.oracle import Oracle, make_params
+    visc, guo, nu_f, f_f, tol = CONVENTIONS[conv]
+    op = make_params(SHAPE, niu=NIU, force=(F, 0.0, 0.0), visc_convention=visc, guo_convention=guo)
+    o = Oracle(op, channel(), precision=64)
+    o.step(20000)
+    v = np.asarray(o.field("v"))
+    vx = v[0, 1:-1, 0, 0]
+    assert rel_err(vx, analytic(nu_f, f_f)) < tol
+    # the profile is the same in every x, z column and has no y/z component
+    assert np.allclose(v[..., 0][:, 1:-1, :], vx[None, :, None], rtol=1e-12, atol=0)
+    assert np.abs(v[..., 1:]).max() < 1e-6 * np.abs(vx).max()
+
+
+# storage -> tolerance of the standard-convention profile on the GPU.  FP64
+# and the FP32 deviation form reproduce the parabola; FP32 reference
+# arithmetic carries the reference's own round-off (f ~ w, |u| ~ 3e-4: 0.9%,
+# the same as the FP32 oracle).  The 16-bit storages are regression bounds,
+# not accuracy claims: at steady state each step's forcing changes the stored
+# deviation by about 8 nu / H^2 ~ 3e-3 of itself, a few FP16 ulps and about
+# one BF16 ulp, so rounding stalls the profile (measured 3.8% and 31%).
+GPU_TOL = {"f64": 1e-8, "f32dev": 1e-3, "f32": 2e-2, "f16": 6e-2, "bf16": 0.4}
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("storage", list(GPU_TOL))
+def test_gpu_channel_flow_matches_parabola(storage):
+    from taichi_lbm3d_gb300 import _native
+    visc, guo, nu_f, f_f, _ = CONVENTIONS["standard"]
+    p = _native.make_params(SHAPE, niu=NIU, force=(F, 0.0, 0.0), visc_convention=visc, guo_convention=guo,
+                            storage=storage)
+    lat = _native.Lattice(p)
+    lat.set_geometry(channel())
+    lat.init()
+    lat.step(20000)
+    rho, v = lat.macros_f64() if storage == "f64" else lat.macros()
+    lat.close()
+    vx = np.asarray(v, np.float64)[0, 1:-1, 0, 0]
+    err = rel_err(vx, analytic(nu_f, f_f))
+    print("%s: max relative error %.3e" % (storage, err))
+    assert err < GPU_TOL[storage]
