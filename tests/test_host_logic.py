@@ -123,3 +123,11 @@ def test_voxelize_cli_rejects_missing_file(tmp_path):
     bad.write_text("not a mesh")
     with pytest.raises(ValueError):
         vx.read_stl(str(bad))
+
+
+def test_unet_rejects_unknown_activation():
+    pytest.importorskip("torch")
+    from taichi_lbm3d_gb300.unet import ACTIVATIONS, UNet3D
+    assert ACTIVATIONS == {"relu": 0, "gelu": 1}
+    with pytest.raises(ValueError):
+        UNet3D(seed=0, activation="tanh")
