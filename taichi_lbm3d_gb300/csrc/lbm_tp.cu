@@ -282,8 +282,11 @@ __device__ __forceinline__ void colour_pull_one(const TpConsts<R>& T, const int3
     acc_b = acc_b + gb;
 }
 
+// 4 CTAs of 256 per SM (64 registers): the 19 source gathers of 6 values each
+// stay in flight together; at the compiler's own 40 registers (6 CTAs) the
+// 131^3 drainage step runs 4.7% slower, at 80 registers (3 CTAs) 23% slower.
 template <typename R>
-__global__ void __launch_bounds__(256) tp_colour_kernel(const __grid_constant__ TpConsts<R> T,
+__global__ void __launch_bounds__(256, 4) tp_colour_kernel(const __grid_constant__ TpConsts<R> T,
                                                         const R* __restrict__ rr_in, const R* __restrict__ rb_in,
                                                         const R* __restrict__ v, const R* __restrict__ cs,
                                                         R* __restrict__ rr_out, R* __restrict__ rb_out,
