@@ -103,8 +103,12 @@ __device__ __forceinline__ void grey_face_restore(R* F, int i, int j, int k, con
 #undef LBM_R
 }
 
+// 4 CTAs of 256 per SM (64 registers); the density-referenced 16-bit codecs,
+// which gather the source densities as well, 3 (80 registers): on the 256^3
+// grey field FP16 runs 25.7k MLUPS at 3 against 24.4k at 4, while FP32 and
+// f32dev lose 6% and 11% at 3.
 template <int STORE, bool FORCE, bool MACROS>
-__global__ void __launch_bounds__(256, STORE == LBM_STORE_F64 ? 1 : 4) grey_step_kernel(
+__global__ void __launch_bounds__(256, STORE == LBM_STORE_F64 ? 1 : (Codec<STORE>::RHOREF ? 3 : 4)) grey_step_kernel(
     const __grid_constant__ SpConsts<typename Codec<STORE>::R> C, const typename Codec<STORE>::T* __restrict__ fin,
     typename Codec<STORE>::T* __restrict__ fout, const int32_t* __restrict__ map, const uint32_t* __restrict__ coord,
     const typename Codec<STORE>::R* __restrict__ ns, typename Codec<STORE>::R* __restrict__ face_stale,
