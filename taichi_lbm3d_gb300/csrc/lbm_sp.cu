@@ -274,6 +274,7 @@ template SpConsts<float> sp_make_consts<float>(const LbmHandle*);
 template SpConsts<double> sp_make_consts<double>(const LbmHandle*);
 
 int sp_launch_steps(LbmHandle* h, int32_t n, bool macros_last) {
+    if (h->n_fluid == 0) return LBM_OK;   // all solid: nothing to update (an empty grid is not launchable)
     if (h->grey) return grey_launch_steps(h, n, macros_last);
     switch (h->p.storage) {
     case LBM_STORE_F32: return run_steps<LBM_STORE_F32>(h, n, macros_last);
@@ -286,6 +287,7 @@ int sp_launch_steps(LbmHandle* h, int32_t n, bool macros_last) {
 }
 
 int sp_launch_init(LbmHandle* h, const void* rho_nodes, const void* v_nodes) {
+    if (h->n_fluid == 0) return LBM_OK;
     const float* r = (const float*)rho_nodes;
     const float* v = (const float*)v_nodes;
     switch (h->p.storage) {
@@ -299,6 +301,7 @@ int sp_launch_init(LbmHandle* h, const void* rho_nodes, const void* v_nodes) {
 }
 
 int sp_launch_debug_stream(LbmHandle* h, const float* d_in, float* d_out) {
+    if (h->n_fluid == 0) return LBM_OK;
     const SpConsts<float> C = sp_make_consts<float>(h);
     const int grid = (int)((h->n_fluid + h->block - 1) / h->block);
     sp_gather_kernel<<<grid, h->block, 0, h->stream>>>(C, d_in, d_out, h->d_map, h->d_coord);

@@ -486,6 +486,11 @@ int tp_steps_t(LbmHandle* h, int32_t nsteps) {
 }  // namespace
 
 int tp_launch_init(LbmHandle* h) {
+    if (h->n_fluid == 0) {   // all solid: nothing to initialise (an empty grid is not launchable)
+        h->cur = 0;
+        h->ccur = 0;
+        return LBM_OK;
+    }
     switch (h->p.storage) {
     case LBM_STORE_F32: return tp_init_t<LBM_STORE_F32>(h);
     case LBM_STORE_F16_DEV: return tp_init_t<LBM_STORE_F16_DEV>(h);
@@ -497,6 +502,7 @@ int tp_launch_init(LbmHandle* h) {
 }
 
 int tp_launch_steps(LbmHandle* h, int32_t n, bool) {
+    if (h->n_fluid == 0) return LBM_OK;
     switch (h->p.storage) {
     case LBM_STORE_F32: return tp_steps_t<LBM_STORE_F32>(h, n);
     case LBM_STORE_F16_DEV: return tp_steps_t<LBM_STORE_F16_DEV>(h, n);
