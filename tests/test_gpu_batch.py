@@ -87,3 +87,25 @@ def test_batch_beyond_int32_population_offsets():
     lat.close()
     assert np.array_equal(rho_s, rho_r) and np.array_equal(v_s, v_r)
     assert np.all(rho_b == rho_b.flat[0]) and np.all(v_b[..., 0] == v_b.flat[0]) and v_b.flat[0] > 0
+
+
+def test_batch_with_an_all_solid_subvolume():
+    """A subvolume without fluid rides along: zero Darcy velocity, converged at
+    its second check, rho = 1 / v = 0 everywhere; the others are unaffected."""
+    from taichi_lbm3d_gb300.batch import Batch
+    S = solids()
+    S.insert(1, np.ones((12, 10, 8), np.int8))
+    b = Batch(S, niu=0.1, force=(1e-5, 0, 0), storage="f32")
+    b.configure([64, 64, 128, 32], 128)
+    b.init()
+    darcy, steps, conv = b.run_to_convergence(tol=0.0, check_every=50, max_steps=100)
+    assert darcy[1] == 0.0 and conv[1] and steps[1] == 100
+    rho, v = b.macros(1)
+    assert np.all(rho == 1.0) and np.all(v == 0.0)
+    ref = Batch([S[0]], niu=0.1, force=(1e-5, 0, 0), storage="f32")
+    ref.configure([64], 128)
+    ref.init()
+    d0, _, _ = ref.run_to_convergence(tol=0.0, check_every=50, max_steps=100)
+    assert abs(darcy[0] - d0[0]) <= 1e-12 * abs(d0[0])
+    ref.close()
+    b.close()
