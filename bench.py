@@ -19,6 +19,7 @@ Under torchrun (N > 1) every rank runs its own replica (the path is replicated,
 not sharded: there is no exchange step).
 """
 import argparse
+import importlib.util
 import json
 import os
 import re
@@ -629,7 +630,8 @@ def main():
                 "cpu_baseline": cb,
                 "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
                 "note": "the reference's Taichi ti.cpu path is not installable offline; this is the C oracle "
-                        "restating its four-sweep algorithm"}
+                        "restating its four-sweep algorithm",
+                "taichi_importable": importlib.util.find_spec("taichi") is not None}
         print(json.dumps(line))
         return 0
 
