@@ -308,8 +308,8 @@ def batched(n_sub=256, seeds0=4000, fp64_subset=16, storage="f16", tol=1e-6, che
             "k_rel_err_serial_f32_vs_f64_median": float(np.median(err_s))}
 
 
-def two_phase(steps=20000, every=500, shape=(131, 131, 131), storages=("f64", "f32", "f16"),
-              log=lambda m: print(m, file=sys.stderr, flush=True)):
+def two_phase(steps=20000, every=500, shape=(131, 131, 131), storages=("f64", "f32", "f16"), cpu=True,
+              cpu_seconds=20.0, log=lambda m: print(m, file=sys.stderr, flush=True)):
     """Config 3: colour-gradient drainage on a 131^3 pack (seed 3, r U[3,8],
     phi 0.40), psi = -1 with a 5-node psi = +1 slab at x-left, constant psi +1 /
     -1 and pressure 1.001 / 1.0 on the x faces, periodic y/z, CapA 0.005,
@@ -373,6 +373,24 @@ def two_phase(steps=20000, every=500, shape=(131, 131, 131), storages=("f64", "f
         out["interface_max_abs_err_" + sto] = float(np.nanmax(np.abs(pa - p64)))
     out["saturation_f64"] = [float(x) for x in s64]
     out["interface_f64"] = [float(x) for x in p64]
+    if cpu:
+        # the C oracle's two-phase step (reference algorithm) on a bounded sample of the same lattice
+        from oracle.oracle import Oracle, make_params
+        p = make_params(shape, bc=(1, 1, 0, 0, 0, 0), rho_bc=(1.001, 1.0, 1, 1, 1, 1), visc_convention=1,
+                        guo_convention=1, bc_form=1, two_phase=True, niu_l=0.05, niu_g=0.2, psi_solid=0.7,
+                        cap_a=0.005, psi_bc=(1, 1, 0, 0, 0, 0), psi_val=(1.0, -1.0, 1, 1, 1, 1))
+        o = Oracle(p, solid, psi0)
+        o.step(1)
+        n, t = 0, 0.0
+        while t < cpu_seconds and n < 100:
+            t0 = time.perf_counter()
+            o.step(1)
+            t += time.perf_counter() - t0
+            n += 1
+        o.close()
+        out["cpu_baseline"] = {"value": out["n_fluid"] * n / t / 1e6, "unit": UNIT,
+                               "cores": len(os.sched_getaffinity(0)), "kind": "port",
+                               "sample": "%d two-phase steps of the full %d^3 lattice (%.1f s)" % (n, shape[0], t)}
     return out
 
 
@@ -599,7 +617,7 @@ def main():
         print(json.dumps({"grey": grey(steps=a.steps or 1000, cpu=not a.no_cpu_baseline)}))
         return 0
     if a.two_phase:
-        print(json.dumps({"two_phase": two_phase(steps=a.steps or 20000)}))
+        print(json.dumps({"two_phase": two_phase(steps=a.steps or 20000, cpu=not a.no_cpu_baseline)}))
         return 0
     if a.steps is None:
         a.steps = 2000
