@@ -224,6 +224,15 @@ int lbm_batch_info(LbmBatch* b, int64_t* n_nodes, int64_t* n_fluid, int32_t* gri
  * when h is NULL) into buf. */
 int lbm_last_error(LbmHandle* h, char* buf, size_t n);
 
+/* Replaces the np.loadtxt inside init_geo (SP:173-177; the two-phase and grey
+ * scripts' geometry/psi/ns files): the whitespace-separated numbers of an ASCII
+ * file, parsed on the host in parallel, needs no GPU.  *count = how many the
+ * file holds; with out non-NULL the file must hold exactly n (else LBM_EINVAL)
+ * and they are written to out as double, rounded as np.loadtxt rounds them.  A
+ * token that is not a number (comments included) is LBM_EINVAL with its byte
+ * offset in the message (lbm_last_error(NULL, ...)). */
+int lbm_read_ascii(const char* path, double* out, int64_t n, int64_t* count);
+
 /* No counterpart in the reference.  The FP64 reduction of lbm_reductions for
  * callers that cannot allocate device memory: a host framework whose own pool
  * allocator already owns the GPU's memory, or a time-critical loop that must not

@@ -85,6 +85,7 @@ SIGNATURES = {
     "lbm_set_populations": [_P, _P],
     "lbm_debug_stream": [_P, _P, _P],
     "lbm_last_error": [_P, ctypes.c_char_p, ctypes.c_size_t],
+    "lbm_read_ascii": [ctypes.c_char_p, _P, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)],
 }
 
 _lib = None
@@ -106,6 +107,21 @@ def load(path=LIB_PATH):
             raise LbmError(LBM_EINVAL, "ABI version mismatch")
         _lib = L
     return _lib
+
+
+def read_ascii(path, n=None):
+    """Whitespace-separated numbers of an ASCII file as float64, parsed by the
+    library on the host (lbm_read_ascii); n, when given, is the count the file
+    must hold."""
+    L = load()
+    cnt = ctypes.c_int64(0)
+    p = os.fsencode(path)
+    if n is None:
+        check(L.lbm_read_ascii(p, None, 0, ctypes.byref(cnt)))
+        n = cnt.value
+    out = np.empty(int(n), np.float64)
+    check(L.lbm_read_ascii(p, ptr(out), int(n), ctypes.byref(cnt)))
+    return out
 
 
 def last_error(h=None):

@@ -17,8 +17,8 @@ import numpy as np
 
 def read_ascii_geometry(filename, shape):
     """Solid mask (int8, shape (nx,ny,nz)) from an ASCII 0/1 file, x fastest."""
-    vals = _read_numbers(filename)
     n = int(np.prod(shape))
+    vals = _read_numbers(filename, n)
     if vals.size != n:
         raise ValueError("%s holds %d values, lattice %s needs %d" % (filename, vals.size, shape, n))
     solid = (vals > 0).astype(np.int8)
@@ -28,8 +28,8 @@ def read_ascii_geometry(filename, shape):
 def read_ascii_field(filename, shape, dtype=np.float32):
     """Field of the lattice shape from an ASCII file, x fastest (float32 unless
     ``dtype`` says otherwise; np.loadtxt's float64 for the grey-scale ns)."""
-    vals = _read_numbers(filename)
     n = int(np.prod(shape))
+    vals = _read_numbers(filename, n)
     if vals.size != n:
         raise ValueError("%s holds %d values, lattice %s needs %d" % (filename, vals.size, shape, n))
     return vals.astype(dtype).reshape(shape, order="F")
@@ -40,10 +40,21 @@ def write_ascii_geometry(filename, solid, fmt="%d"):
     np.savetxt(filename, a, fmt=fmt)
 
 
-def _read_numbers(filename):
+def _read_numbers(filename, n=None):
+    """All numbers of the file, as np.loadtxt would read them (float64): the
+    library's parallel parser (lbm_read_ascii) when it is built, else numpy.
+    Reading is host work; no GPU is involved either way.  With n given, a file
+    holding another count raises ValueError."""
+    from . import _native
+    try:
+        return _native.read_ascii(filename, n)
+    except _native.LbmError as e:
+        if e.code != _native.LBM_ENODEV:      # the file itself is bad
+            raise ValueError(str(e)) from None
+    except OSError:                           # library present but not loadable here
+        pass
     with open(filename, "rb") as fh:
         data = fh.read()
-    # fast path: whitespace-separated decimal numbers
     return np.array(data.split(), dtype=np.float64)
 
 
