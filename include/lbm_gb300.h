@@ -157,6 +157,8 @@ int lbm_get_macros_f64(LbmHandle* h, double* rho, double* v);
 
 /* Two-phase fields after the last step: psi, rho_r, rho_b (dense; NULL to skip). */
 int lbm_get_phase(LbmHandle* h, float* psi, float* rho_r, float* rho_b);
+/* psi alone (the two-phase script's psi.to_numpy()): lbm_get_phase(h, psi, NULL, NULL). */
+int lbm_get_psi(LbmHandle* h, float* psi);
 
 /* get_max_v / cal_max_v (SP:394-402): max |v| over all cells. */
 int lbm_get_max_v(LbmHandle* h, float* out);

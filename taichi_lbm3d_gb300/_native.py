@@ -86,6 +86,7 @@ SIGNATURES = {
     "lbm_debug_stream": [_P, _P, _P],
     "lbm_last_error": [_P, ctypes.c_char_p, ctypes.c_size_t],
     "lbm_read_ascii": [ctypes.c_char_p, _P, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)],
+    "lbm_get_psi": [_P, _P],
 }
 
 _lib = None
@@ -234,6 +235,11 @@ class Lattice:
         out = [np.empty(self.ncell, np.float32) for _ in range(3)]
         self._c(load().lbm_get_phase(self.h, *[ptr(a) for a in out]))
         return tuple(a.reshape(self.shape, order="F") for a in out)
+
+    def psi(self):
+        out = np.empty(self.ncell, np.float32)
+        self._c(load().lbm_get_psi(self.h, ptr(out)))
+        return out.reshape(self.shape, order="F")
 
     def max_v(self):
         f = ctypes.c_float()

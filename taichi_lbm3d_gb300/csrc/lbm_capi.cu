@@ -469,6 +469,11 @@ int lbm_get_macros_f64(LbmHandle* h, double* rho, double* v) {
     return rc;
 }
 
+int lbm_get_psi(LbmHandle* h, float* psi) {
+    if (!psi) return lbm_set_err(h, LBM_EINVAL, "lbm_get_psi: NULL output");
+    return lbm_get_phase(h, psi, nullptr, nullptr);
+}
+
 int lbm_get_phase(LbmHandle* h, float* psi, float* rho_r, float* rho_b) {
     if (!h) return lbm_set_err(h, LBM_EINVAL, "lbm_get_phase: NULL handle");
     if (!h->p.two_phase) return lbm_set_err(h, LBM_ESTATE, "lbm_get_phase: handle is single phase");

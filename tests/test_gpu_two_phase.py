@@ -83,7 +83,9 @@ def test_drainage_200_steps_bit_exact():
     op, solid, psi0 = drainage_case()
     o = Oracle(op, solid, psi0)
     o.step(200)
-    g = gpu_fields(run_gpu(op, solid, psi0, 200))
+    lat = run_gpu(op, solid, psi0, 200)
+    g = gpu_fields(lat)
+    assert np.array_equal(lat.psi(), g["psi"])            # lbm_get_psi == lbm_get_phase's psi
     fl = solid == 0
     for f in FIELDS:
         assert np.array_equal(g[f][fl], o.field(f).astype(np.float32)[fl]), f
