@@ -33,9 +33,11 @@
 
 // Resident 256-thread CTAs per SM requested for the step kernel (caps
 // registers at 65536 / (256 * n)).  The reference-arithmetic FP32 kernel is
-// fastest at 6 (40 registers); the deviation-form kernels, whose pair-form
-// transforms keep more values live, spill at 6 and are fastest at 5
-// (measured on the 256^3 pack: f32dev +4%, FP16 +8%, BF16 +13% over 6).
+// fastest at 6 (40 registers), 4 with the dense Guo forcing; the
+// deviation-form kernels, whose pair-form transforms keep more values live,
+// spill at 6 and are fastest at 5, forced or not (measured on the 256^3 pack:
+// unforced f32dev +4%, FP16 +8%, BF16 +13% over 6; forced +1%, +7%, +4%
+// over 4).
 #ifndef LBM_SP_MINBLOCKS
 #define LBM_SP_MINBLOCKS 6
 #endif
@@ -104,8 +106,8 @@ __device__ __forceinline__ void sp_finish_node(typename Codec<STORE>::R* F, int 
 
 template <int STORE, bool FORCE, bool MACROS>
 __global__ void __launch_bounds__(256, STORE == LBM_STORE_F64 ? 1
-                                           : FORCE                ? 4
                                            : Codec<STORE>::DEV    ? LBM_SP_MINBLOCKS_DEV
+                                           : FORCE                ? 4
                                                                   : LBM_SP_MINBLOCKS)
     sp_step_kernel(const __grid_constant__ SpConsts<typename Codec<STORE>::R> C,
                                                       const typename Codec<STORE>::T* __restrict__ fin,
