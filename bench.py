@@ -208,7 +208,7 @@ def cpu_baseline(solid, max_seconds=20.0):
 
 def convergence(storages=("f64", "f32", "f32dev", "f16", "bf16"), tol=1e-6, check_every=500, max_steps=200_000,
                 shape=SHAPE, visc="standard"):
-    """Config 2 run to steady state: |dk/k| <= tol over check_every steps.
+    """The 256^3 pack run to steady state: |dk/k| <= tol over check_every steps.
     Each storage variant reports steps, wall time and its permeability error
     against the FP64 run of the same solver."""
     from taichi_lbm3d_gb300 import LB3D_Solver_Single_Phase
@@ -239,14 +239,14 @@ def convergence(storages=("f64", "f32", "f32dev", "f16", "bf16"), tol=1e-6, chec
 
 def batched(n_sub=256, seeds0=4000, fp64_subset=16, storage="f16", tol=1e-6, check_every=500,
             max_steps=100_000, log=lambda m: print(m, file=sys.stderr, flush=True)):
-    """Config 4: n_sub seeded subvolumes (edges {48..160}, r U[3,8], phi
+    """Batched permeability: n_sub seeded subvolumes (edges {48..160}, r U[3,8], phi
     U[0.25,0.5]), fx = 1e-6, periodic, niu 0.1, each to steady state:
     one persistent graph-captured batch (autotuned) against a serial loop of the
     plain FP32 kernel; per-sample k error against FP64 on a subset."""
     from taichi_lbm3d_gb300 import autotune
-    from taichi_lbm3d_gb300.batch import Batch, config4_solids
+    from taichi_lbm3d_gb300.batch import Batch, subvolume_solids
     t0 = time.perf_counter()
-    solids = config4_solids(range(seeds0, seeds0 + n_sub))          # spawned pool, before CUDA
+    solids = subvolume_solids(range(seeds0, seeds0 + n_sub))          # spawned pool, before CUDA
     log("generated %d subvolumes in %.1f s" % (n_sub, time.perf_counter() - t0))
     edges = [s.shape[0] for s in solids]
     by_edge = {}
@@ -310,7 +310,7 @@ def batched(n_sub=256, seeds0=4000, fp64_subset=16, storage="f16", tol=1e-6, che
 
 def two_phase(steps=20000, every=500, shape=(131, 131, 131), storages=("f64", "f32", "f16"), cpu=True,
               cpu_seconds=20.0, log=lambda m: print(m, file=sys.stderr, flush=True)):
-    """Config 3: colour-gradient drainage on a 131^3 pack (seed 3, r U[3,8],
+    """Two-phase colour-gradient drainage on a 131^3 pack (seed 3, r U[3,8],
     phi 0.40), psi = -1 with a 5-node psi = +1 slab at x-left, constant psi +1 /
     -1 and pressure 1.001 / 1.0 on the x faces, periodic y/z, CapA 0.005,
     psi_solid 0.7, niu_l 0.05, niu_g 0.2.  Saturation and interface position
@@ -395,7 +395,7 @@ def two_phase(steps=20000, every=500, shape=(131, 131, 131), storages=("f64", "f
 
 
 def cavity(steps=1000, log=lambda m: print(m, file=sys.stderr, flush=True)):
-    """Config 1: 64^3 lid-driven cavity (one-node solid shell on five faces,
+    """64^3 lid-driven cavity (one-node solid shell on five faces,
     top z face fixed velocity (0.1, 0, 0), niu 0.1, FP32 reference
     arithmetic, class conventions): GPU MLUPS over `steps` steps with CUDA
     events, the CPU oracle over the same steps on all host cores, and the
@@ -595,13 +595,13 @@ def main():
     ap.add_argument("--convergence", action="store_true",
                     help="run the 256^3 pack to steady state in FP64/FP32/FP16/BF16 and print k errors")
     ap.add_argument("--batched", action="store_true",
-                    help="config 4: batched persistent launch vs serial plain kernel, k error vs FP64")
+                    help="256 subvolumes to steady state: batched persistent launch vs serial plain kernel, k error vs FP64")
     ap.add_argument("--n-sub", type=int, default=256)
-    ap.add_argument("--two-phase", action="store_true", help="config 3: two-phase drainage vs FP64")
+    ap.add_argument("--two-phase", action="store_true", help="131^3 two-phase drainage vs FP64")
     ap.add_argument("--grey", action="store_true", help="grey-scale (partial bounce-back) step on a 256^3 grey field")
     ap.add_argument("--voxelize", action="store_true", help="STL voxeliser on a NACA wing in the reference box")
     ap.add_argument("--unet", action="store_true", help="warm-start U-Net training step on 2 x 96^3")
-    ap.add_argument("--cavity", action="store_true", help="config 1: 64^3 lid-driven cavity, GPU vs CPU oracle")
+    ap.add_argument("--cavity", action="store_true", help="64^3 lid-driven cavity, GPU vs CPU oracle")
     a = ap.parse_args()
     if a.cavity:
         print(json.dumps({"cavity": cavity(steps=a.steps or 1000)}))

@@ -124,7 +124,7 @@ class Batch:
         return nu * np.asarray(darcy) / f_eff
 
 
-def config4_sample(seed, edges=(48, 64, 96, 128, 160)):
+def subvolume_sample(seed, edges=(48, 64, 96, 128, 160)):
     """One subvolume of the batched-permeability workload: edge uniform from
     ``edges``, porosity U[0.25, 0.50], sphere radii U[3, 8], percolating."""
     from .geometry import sphere_pack
@@ -134,13 +134,13 @@ def config4_sample(seed, edges=(48, 64, 96, 128, 160)):
     return sphere_pack((edge, edge, edge), 3.0, 8.0, phi, seed)
 
 
-def config4_solids(seeds, workers=None):
+def subvolume_solids(seeds, workers=None):
     """Generate the subvolumes in parallel (spawned processes: call this before
     the first CUDA call of the process)."""
     import multiprocessing as mp
     import os
     workers = workers or max(1, min(16, len(os.sched_getaffinity(0))))
     if workers == 1:
-        return [config4_sample(s) for s in seeds]
+        return [subvolume_sample(s) for s in seeds]
     with mp.get_context("spawn").Pool(workers) as pool:
-        return pool.map(config4_sample, list(seeds), chunksize=1)
+        return pool.map(subvolume_sample, list(seeds), chunksize=1)

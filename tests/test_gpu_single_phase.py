@@ -102,7 +102,7 @@ def test_cavity50_fixture_first_step():
 
 
 def cavity64_params():
-    # BASELINE config 1: 64^3, shell on 5 faces, z-top moving with vx = 0.1, niu = 0.1
+    # the 64^3 lid-driven cavity: shell on 5 faces, z-top moving with vx = 0.1, niu = 0.1
     return oracle_params((64, 64, 64), niu=0.1, bc=(0, 0, 0, 0, 0, 2),
                          vel_bc=((0, 0, 0),) * 5 + ((0.1, 0.0, 0.0),))
 
