@@ -10,6 +10,8 @@ rates satisfy (1/s_v - 1/2)(1/s_q - 1/2) = 3/16 (s_q = 8(2 - s_v)/(8 - s_v),
 SP:131), for which halfway bounce-back gives the parabola exactly, so the
 consistent "standard" pair matches to round-off.  The class and script forms
 shift the velocity by F/2 while injecting F_eff, which leaves a small offset."""
+import functools
+
 import numpy as np
 import pytest
 
@@ -39,14 +41,23 @@ def rel_err(vx, u):
     return float(np.abs(vx - u).max() / np.abs(u).max())
 
 
-@pytest.mark.parametrize("conv", list(CONVENTIONS))
-def test_oracle_channel_flow_matches_parabola(conv):
+@functools.lru_cache(maxsize=None)
+def oracle_velocity(conv):
+    """v of the FP64 oracle after 20,000 steps of the channel (shared by the tests)."""
     from oracle.oracle import Oracle, make_params
-    visc, guo, nu_f, f_f, tol = CONVENTIONS[conv]
+    visc, guo = CONVENTIONS[conv][:2]
     op = make_params(SHAPE, niu=NIU, force=(F, 0.0, 0.0), visc_convention=visc, guo_convention=guo)
     o = Oracle(op, channel(), precision=64)
     o.step(20000)
-    v = np.asarray(o.field("v"))
+    v = np.array(o.field("v"))
+    o.close()
+    return v
+
+
+@pytest.mark.parametrize("conv", list(CONVENTIONS))
+def test_oracle_channel_flow_matches_parabola(conv):
+    visc, guo, nu_f, f_f, tol = CONVENTIONS[conv]
+    v = oracle_velocity(conv)
     vx = v[0, 1:-1, 0, 0]
     assert rel_err(vx, analytic(nu_f, f_f)) < tol
     # the profile is the same in every x, z column and has no y/z component
@@ -81,3 +92,20 @@ def test_gpu_channel_flow_matches_parabola(storage):
     err = rel_err(vx, analytic(nu_f, f_f))
     print("%s: max relative error %.3e" % (storage, err))
     assert err < GPU_TOL[storage]
+
+
+@pytest.mark.parametrize("conv", list(CONVENTIONS))
+def test_permeability_of_the_channel(conv):
+    """The class's permeability formula (Darcy velocity over all cells, nu_eff and
+    F_eff of the conventions) applied to the oracle's steady channel gives the
+    slit's permeability, sum over fluid rows of (y - 1/2)(ny - 3/2 - y) / 2, / ny."""
+    from taichi_lbm3d_gb300 import LB3D_Solver_Single_Phase
+    visc, guo, _, _, tol = CONVENTIONS[conv]
+    names = {0: "class", 1: "standard"}[visc], {0: "class", 1: "script", 2: "standard"}[guo]
+    darcy = float(oracle_velocity(conv)[..., 0].sum()) / np.prod(SHAPE)
+    lb = LB3D_Solver_Single_Phase(*SHAPE, viscosity_convention=names[0], guo_convention=names[1])
+    lb.niu, lb.fx = NIU, F
+    lb.tau_f = NIU / 3.0 + 0.5 if names[0] == "class" else 3.0 * NIU + 0.5   # as init_simulation sets it
+    y = np.arange(1, NY - 1, dtype=np.float64)
+    k_slit = float(((y - 0.5) * (NY - 1.5 - y) / 2.0).sum()) / NY
+    assert abs(lb._k_from_darcy(darcy, 0) - k_slit) < tol * k_slit
