@@ -131,3 +131,38 @@ def test_unet_rejects_unknown_activation():
     assert ACTIVATIONS == {"relu": 0, "gelu": 1}
     with pytest.raises(ValueError):
         UNet3D(seed=0, activation="tanh")
+
+
+def test_two_phase_saturation_and_interface_position():
+    """Host-side diagnostics of the two-phase class on a synthetic psi field:
+    saturation = share of fluid cells with psi > 0, interface = mean x of the
+    sign changes along x between fluid cells (cell faces at x + 1/2)."""
+    from taichi_lbm3d_gb300 import LB3D_Solver_Two_Phase
+    s = LB3D_Solver_Two_Phase(8, 3, 2)
+    solid = np.zeros((8, 3, 2), np.int8)
+    solid[:, 0, :] = 1                                   # one solid row: 8 x 2 x 2 = 32 fluid cells
+    s.solid.from_numpy(solid)
+    psi = -np.ones((8, 3, 2), np.float32)
+    psi[:3] = 1.0                                        # invading phase in x = 0, 1, 2
+    psi[:5, 2, 1] = 1.0                                  # one row reaches x = 4
+    s._phase = lambda: (psi, None, None)
+    assert s.saturation() == (3 * 4 + 2) / 32
+    assert s.interface_position() == (3 * 2.5 + 4.5) / 4
+    psi[:] = -1.0
+    assert s.saturation() == 0.0 and np.isnan(s.interface_position())
+
+
+def test_warmstart_summary():
+    from taichi_lbm3d_gb300.warmstart import summarize
+    rows = []
+    for q, (rest_s, warm_s, rest_st, warm_st, r16_st) in enumerate(
+            [(10.0, 2.0, 10000, 3000, 3500), (4.0, 1.0, 4000, 2000, 2000), (6.0, 3.0, 6000, 2500, 2000)]):
+        rows.append({"rest_f32_seconds": rest_s, "warm_f16_seconds": warm_s, "rest_f32_steps": rest_st,
+                     "warm_f16_steps": warm_st, "rest_f16_steps": r16_st, "warm_v_f16_steps": warm_st,
+                     "speedup_warm_f16_vs_rest_f32": rest_s / warm_s,
+                     "step_ratio_warm_vs_rest_f16": r16_st / warm_st, "step_ratio_warm_v_vs_rest_f16": r16_st / warm_st})
+    rows[0]["warm_f16_k_err"] = 1e-5
+    sm = summarize(rows)
+    assert sm["n"] == 3 and sm["speedup_total"] == 20.0 / 6.0 and sm["speedup_median"] == 4.0
+    assert (sm["warm_fewer_steps"], sm["warm_more_steps"]) == (1, 1)
+    assert sm["k_err_warm_f16_vs_f64_max"] == 1e-5 and sm["k_err_rest_f32_vs_f64_max"] is None
