@@ -34,6 +34,24 @@ E = np.array([[0, 0, 0], [1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0], [0, 0, 1]
               [0, -1, -1], [0, 1, -1], [0, -1, 1]], dtype=np.int32)
 W = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12, dtype=np.float32)
 LR = [0, 2, 1, 4, 3, 6, 5, 8, 7, 10, 9, 12, 11, 14, 13, 16, 15, 18, 17]
+_MOMENTS = None
+
+
+def moment_matrices():
+    """M and inv_M as the reference's class holds them (SP:61-110): M of the
+    kernels' generator (csrc/gen_mrt.py) in FP32, and inv(M) taken in FP64 and
+    stored as FP32 (Q14)."""
+    global _MOMENTS
+    if _MOMENTS is None:
+        import importlib.util
+        import os
+        path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "csrc", "gen_mrt.py")
+        spec = importlib.util.spec_from_file_location("_lbm_gen_mrt", path)
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        m = np.array(mod.M, dtype=np.float64)
+        _MOMENTS = (m.astype(np.float32), np.linalg.inv(m).astype(np.float32))
+    return _MOMENTS[0].copy(), _MOMENTS[1].copy()
 
 
 class LB3D_Solver_Single_Phase:
@@ -66,7 +84,7 @@ class LB3D_Solver_Single_Phase:
         self.e_f = E.astype(np.float32)
         self.w = W.copy()
         self.LR = list(LR)
-        self.M = None
+        self.M, self.inv_M = moment_matrices()
         self.x = np.linspace(0, nx, nx)
         self.y = np.linspace(0, ny, ny)
         self.z = np.linspace(0, nz, nz)

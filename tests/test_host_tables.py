@@ -60,3 +60,13 @@ def test_closed_form_guo_moments_match_the_dense_transform():
             closed[14] = gd * (u[1] * F[2] + u[2] * F[1]) / 9
             closed[15] = gd * (u[0] * F[2] + u[2] * F[0]) / 9
             assert dense == closed
+
+
+def test_class_exposes_the_reference_moment_matrices():
+    """LB3D_Solver_Single_Phase.M / inv_M as the reference holds them: M in FP32
+    and inv(M) computed in FP64, stored in FP32 (SP:61-110)."""
+    from taichi_lbm3d_gb300 import LB3D_Solver_Single_Phase
+    lb = LB3D_Solver_Single_Phase(4, 4, 4)
+    assert lb.M.dtype == np.float32 and np.array_equal(lb.M, M_REF.astype(np.float32))
+    assert lb.inv_M.dtype == np.float32
+    assert np.array_equal(lb.inv_M, np.linalg.inv(M_REF.astype(np.float64)).astype(np.float32))
