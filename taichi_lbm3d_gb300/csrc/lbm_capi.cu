@@ -246,6 +246,7 @@ int lbm_destroy(LbmHandle* h) {
 // built on the device (lbm_geom.cu).  The mask is addressed as
 // solid[i*si + j*sj + k*sk] (element strides).
 int lbm_set_geometry_strided(LbmHandle* h, const int8_t* solid, int64_t si, int64_t sj, int64_t sk) {
+    LbmNvtxRange nvtx("lbm_set_geometry");
     if (!h || !solid) return lbm_set_err(h, LBM_EINVAL, "lbm_set_geometry: NULL argument");
     if (si < 0 || sj < 0 || sk < 0) return lbm_set_err(h, LBM_EINVAL, "lbm_set_geometry: negative stride");
     cudaSetDevice(h->device);
@@ -343,6 +344,7 @@ int lbm_set_psi(LbmHandle* h, const float* psi) {
 }
 
 int lbm_init(LbmHandle* h, const float* rho, const float* v) {
+    LbmNvtxRange nvtx("lbm_init");
     if (!h) return lbm_set_err(h, LBM_EINVAL, "lbm_init: NULL handle");
     if (!h->have_geometry) return lbm_set_err(h, LBM_ESTATE, "lbm_init: call lbm_set_geometry first");
     if ((rho == nullptr) != (v == nullptr)) return lbm_set_err(h, LBM_EINVAL, "lbm_init: give both rho and v, or neither");
@@ -395,6 +397,7 @@ int lbm_init(LbmHandle* h, const float* rho, const float* v) {
 }
 
 int lbm_step_async(LbmHandle* h, int32_t n) {
+    LbmNvtxRange nvtx("lbm_step");
     if (!h) return lbm_set_err(h, LBM_EINVAL, "lbm_step: NULL handle");
     if (!h->initialized) return lbm_set_err(h, LBM_ESTATE, "lbm_step: call lbm_init first");
     if (n < 0) return lbm_set_err(h, LBM_EINVAL, "lbm_step: negative step count");
@@ -439,6 +442,7 @@ int scatter_dense(LbmHandle* h, const void* dsrc, int comps, O* out, O fill) {
 extern "C" {
 
 int lbm_get_macros(LbmHandle* h, float* rho, float* v) {
+    LbmNvtxRange nvtx("lbm_get_macros");
     if (!h) return lbm_set_err(h, LBM_EINVAL, "lbm_get_macros: NULL handle");
     if (!h->have_geometry) return lbm_set_err(h, LBM_ESTATE, "lbm_get_macros: no geometry");
     cudaSetDevice(h->device);
@@ -494,6 +498,7 @@ int lbm_get_phase(LbmHandle* h, float* psi, float* rho_r, float* rho_b) {
 }
 
 int lbm_reductions(LbmHandle* h, LbmStats* out) {
+    LbmNvtxRange nvtx("lbm_reductions");
     if (!h || !out) return lbm_set_err(h, LBM_EINVAL, "lbm_reductions: NULL argument");
     if (!h->have_geometry) return lbm_set_err(h, LBM_ESTATE, "lbm_reductions: no geometry");
     cudaSetDevice(h->device);
@@ -519,6 +524,7 @@ int lbm_get_max_v(LbmHandle* h, float* out) {
 
 int lbm_run_to_convergence(LbmHandle* h, double tol, int32_t check_every, int64_t max_steps, int32_t axis,
                            double* darcy_v, int64_t* steps, int32_t* converged) {
+    LbmNvtxRange nvtx("lbm_run_to_convergence");
     if (!h || !darcy_v || !steps || !converged) return lbm_set_err(h, LBM_EINVAL, "lbm_run_to_convergence: NULL argument");
     if (check_every < 1 || max_steps < 1 || axis < 0 || axis > 2 || !(tol >= 0))
         return lbm_set_err(h, LBM_EINVAL, "lbm_run_to_convergence: bad tol / check_every / max_steps / axis");

@@ -8,6 +8,18 @@
 
 #include "../../include/lbm_gb300.h"
 
+#include <nvtx3/nvToolsExt.h>
+
+// NVTX range over one C ABI call (header-only NVTX; a no-op unless a profiler
+// such as Nsight attaches), so a timeline shows where the host calls start and
+// end: "lbm_step", "lbm_run_to_convergence", "lbm_set_geometry", ...
+struct LbmNvtxRange {
+    explicit LbmNvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~LbmNvtxRange() { nvtxRangePop(); }
+    LbmNvtxRange(const LbmNvtxRange&) = delete;
+    LbmNvtxRange& operator=(const LbmNvtxRange&) = delete;
+};
+
 // Per-launch constants of the single-phase step (template on compute type R).
 template <typename R>
 struct SpConsts {

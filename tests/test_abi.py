@@ -66,3 +66,28 @@ def test_create_without_gpu_fails_loudly(lib):
     with pytest.raises(_native.LbmError) as ei:
         _native.Lattice(_native.make_params((8, 8, 8)))
     assert ei.value.code == _native.LBM_ENODEV
+
+
+def test_null_handles_are_rejected_without_a_gpu(lib):
+    """Host-side failure paths: every handle call given NULL returns LBM_EINVAL
+    (and records a message) before touching CUDA; the NVTX ranges around the
+    calls are inert without a profiler."""
+    P = ctypes.c_void_p
+    lib.lbm_step_async.argtypes = [P, ctypes.c_int32]
+    lib.lbm_step.argtypes = [P, ctypes.c_int32]
+    lib.lbm_init.argtypes = [P, P, P]
+    lib.lbm_get_macros.argtypes = [P, P, P]
+    lib.lbm_reductions.argtypes = [P, P]
+    lib.lbm_set_geometry_strided.argtypes = [P, P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64]
+    lib.lbm_run_to_convergence.argtypes = [P, ctypes.c_double, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32,
+                                           P, P, P]
+    lib.lbm_last_error.argtypes = [P, ctypes.c_char_p, ctypes.c_size_t]
+    calls = [lambda: lib.lbm_step_async(None, 1), lambda: lib.lbm_step(None, 1),
+             lambda: lib.lbm_init(None, None, None), lambda: lib.lbm_get_macros(None, None, None),
+             lambda: lib.lbm_reductions(None, None), lambda: lib.lbm_set_geometry_strided(None, None, 1, 1, 1),
+             lambda: lib.lbm_run_to_convergence(None, 1e-6, 10, 10, 0, None, None, None)]
+    for c in calls:
+        assert c() == -1
+    buf = ctypes.create_string_buffer(256)
+    lib.lbm_last_error(None, buf, 256)
+    assert b"NULL" in buf.value
