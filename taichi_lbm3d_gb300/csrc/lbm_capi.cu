@@ -412,7 +412,8 @@ int lbm_step_async(LbmHandle* h, int32_t n) {
 
 int lbm_synchronize(LbmHandle* h) {
     if (!h) return lbm_set_err(h, LBM_EINVAL, "lbm_synchronize: NULL handle");
-    return lbm_cuda_check(h, cudaStreamSynchronize(h->stream), "stream synchronize");
+    const int rc = lbm_cuda_check(h, cudaStreamSynchronize(h->stream), "stream synchronize");
+    return rc ? rc : sp_debug_take(h);
 }
 
 int lbm_step(LbmHandle* h, int32_t n) {

@@ -107,6 +107,8 @@ SpConsts<R> sp_make_consts(const LbmHandle* h);
 
 // grey scale (lbm_grey.cu)
 int grey_launch_steps(LbmHandle* h, int32_t n, bool macros_last);
+// Result of the -DLBM_DEBUG index checks since the last call (LBM_OK in other builds).
+int sp_debug_take(LbmHandle* h);
 
 // two phase (lbm_tp.cu)
 int tp_launch_init(LbmHandle* h);

@@ -43,6 +43,18 @@ __device__ __forceinline__ int pull_source(const int32_t* __restrict__ map, cons
     }
 }
 
+#ifdef LBM_DEBUG
+// Debug builds (-DLBM_DEBUG): the first failed index check is recorded here
+// (1 = node coordinates outside the lattice, 2 = a map entry beyond the
+// fluid-node count) and read back by the host after the step; the offending
+// access is skipped.  One copy per translation unit; the single-phase step
+// (lbm_sp.cu) sets the node limit and reads the flag; elsewhere the limit
+// stays 0 and the check is off.
+static __device__ int g_lbm_debug;
+static __device__ int g_lbm_debug_nlimit;
+__device__ __forceinline__ void lbm_debug_fail(int code) { atomicCAS(&g_lbm_debug, 0, code); }
+#endif
+
 template <int STORE, bool XWRAP>
 struct Gather {
     using Cd = Codec<STORE>;
@@ -52,7 +64,15 @@ struct Gather {
     static __device__ __forceinline__ void one(R* F, const T* __restrict__ fin, const T* __restrict__ own,
                                                const int32_t* __restrict__ map, const Rows& rows, int i, int xm,
                                                int xp, const float* __restrict__ rref, int n) {
+#ifdef LBM_DEBUG
+        int src = pull_source<S, XWRAP>(map, rows, i, xm, xp);
+        if (g_lbm_debug_nlimit > 0 && src >= g_lbm_debug_nlimit) {
+            lbm_debug_fail(2);
+            src = -1;
+        }
+#else
         const int src = pull_source<S, XWRAP>(map, rows, i, xm, xp);
+#endif
         if (src >= 0) F[S] = Cd::template dec<S>(fin[lbm_eoff32(src) + 32 * S]);
         else F[S] = Cd::template dec<S>(own[32 * lbm_lr(S)]);
         if constexpr (Cd::RHOREF) F[S] = lbm_fma<R>((R)lbm_w(S), (R)rref[src >= 0 ? src : n], F[S]);

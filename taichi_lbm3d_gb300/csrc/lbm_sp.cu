@@ -129,6 +129,12 @@ __global__ void __launch_bounds__(256, STORE == LBM_STORE_F64 ? 1
     if (n >= C.n_fluid) return;
     const uint32_t pc = __ldg(coord + n);   // coordinates and map never change between steps
     const int i = lbm_pi(pc), j = lbm_pj(pc), k = lbm_pk(pc);
+#ifdef LBM_DEBUG
+    if (i >= C.nx || j >= C.ny || k >= C.nz) {
+        lbm_debug_fail(1);
+        return;
+    }
+#endif
 #if LBM_SP_PDL
     // populations, node densities and vprev of the previous step: wait for it
     // to complete (returns at once when launched without the attribute)
@@ -212,6 +218,13 @@ template <int STORE>
 int run_steps(LbmHandle* h, int32_t n, bool macros_last) {
     using R = typename Codec<STORE>::R;
     const SpConsts<R> C = sp_make_consts<R>(h);
+#ifdef LBM_DEBUG
+    int rc0 = lbm_cuda_check(h, cudaMemcpyToSymbolAsync(g_lbm_debug_nlimit, &h->n_fluid, sizeof(int), 0,
+                                                        cudaMemcpyHostToDevice, h->stream),
+                             "debug node limit");
+    if (!rc0) rc0 = lbm_cuda_check(h, cudaStreamSynchronize(h->stream), "debug node limit");
+    if (rc0) return rc0;
+#endif
     const int grid = (int)((h->n_fluid + h->block - 1) / h->block);
     for (int32_t it = 0; it < n; ++it) {
         const bool mac = macros_last && it == n - 1;
@@ -300,6 +313,26 @@ int sp_launch_init(LbmHandle* h, const void* rho_nodes, const void* v_nodes) {
     case LBM_STORE_F64: return run_init<LBM_STORE_F64>(h, r, v);
     }
     return lbm_set_err(h, LBM_EINVAL, "unknown storage");
+}
+
+// Debug builds: the first failed index check since the last call (0 if none),
+// cleared on read.  Other builds: always LBM_OK.
+int sp_debug_take(LbmHandle* h) {
+#ifdef LBM_DEBUG
+    int flag = 0;
+    const int zero = 0;
+    int rc = lbm_cuda_check(h, cudaMemcpyFromSymbol(&flag, g_lbm_debug, sizeof(int)), "debug flag");
+    if (!rc && flag) {
+        rc = lbm_cuda_check(h, cudaMemcpyToSymbol(g_lbm_debug, &zero, sizeof(int)), "debug flag");
+        if (!rc)
+            rc = lbm_set_err(h, LBM_EINVAL, flag == 1 ? "debug check: node coordinates outside the lattice"
+                                                      : "debug check: neighbour map entry beyond the fluid-node count");
+    }
+    return rc;
+#else
+    (void)h;
+    return LBM_OK;
+#endif
 }
 
 int sp_launch_debug_stream(LbmHandle* h, const float* d_in, float* d_out) {
