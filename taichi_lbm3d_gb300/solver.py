@@ -193,12 +193,54 @@ class LB3D_Solver_Single_Phase:
         L = (self.nx, self.ny, self.nz)[axis]
         return self.nu_eff() * vmean * (L - 1) / ((rin - rout) / 3.0)
 
-    def run_to_convergence(self, tol=1e-6, check_every=500, max_steps=1_000_000, axis=0):
+    def run_to_convergence(self, tol=1e-6, check_every=500, max_steps=1_000_000, axis=0, log=None):
         """Step until the permeability changes by <= tol (relative) over
-        ``check_every`` steps; returns dict(k, darcy_v, steps, converged)."""
-        dv, steps, conv = self._need().run_to_convergence(tol, check_every, max_steps, axis)
-        self._cache = None
-        return {"k": self._k_from_darcy(dv, axis), "darcy_v": dv, "steps": steps, "converged": conv}
+        ``check_every`` steps; returns dict(k, darcy_v, steps, converged).
+
+        ``log`` (a path or a writable text file) records one JSON line per check:
+        steps, Darcy velocity, k, its relative change, FP64 mass, max |v|,
+        non-finite count, MLUPS since the start.  Without it the whole loop runs
+        in the library (lbm_run_to_convergence); with it the same loop runs here,
+        one lbm_step + lbm_reductions per check."""
+        if log is None:
+            dv, steps, conv = self._need().run_to_convergence(tol, check_every, max_steps, axis)
+            self._cache = None
+            return {"k": self._k_from_darcy(dv, axis), "darcy_v": dv, "steps": steps, "converged": conv}
+        import json
+        import os
+        import time
+        lat = self._need()
+        if check_every < 1 or max_steps < 1 or axis not in (0, 1, 2) or not tol >= 0:
+            raise ValueError("bad tol / check_every / max_steps / axis")
+        own = isinstance(log, (str, os.PathLike))
+        fh = open(log, "a") if own else log
+        ncell = self.nx * self.ny * self.nz
+        nf = self.n_fluid
+        prev, done, conv, vm = None, 0, False, 0.0
+        t0 = time.perf_counter()
+        try:
+            while done < max_steps:
+                n = min(check_every, max_steps - done)
+                lat.step(n)
+                done += n
+                self._cache = None
+                st = lat.stats()
+                if st.n_nonfinite:
+                    raise _native.LbmError(_native.LBM_EDIVERGED, "run_to_convergence: non-finite rho or v")
+                vm = st.mom[axis] / ncell
+                rel = abs(vm - prev) / abs(vm) if prev is not None and vm != 0 else None
+                fh.write(json.dumps({"steps": done, "darcy_v": vm, "k": self._k_from_darcy(vm, axis),
+                                     "rel_change": rel, "mass": st.mass, "max_v": st.max_v,
+                                     "n_nonfinite": int(st.n_nonfinite),
+                                     "mlups": nf * done / max(time.perf_counter() - t0, 1e-12) / 1e6}) + "\n")
+                if prev is not None and abs(vm - prev) <= tol * abs(vm):
+                    conv = True
+                    break
+                prev = vm
+        finally:
+            if own:
+                fh.close()
+        return {"k": self._k_from_darcy(vm, axis), "darcy_v": vm, "steps": done, "converged": conv}
 
     def export_VTK(self, n):
         rho, v = self._macros()

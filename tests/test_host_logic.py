@@ -166,3 +166,39 @@ def test_warmstart_summary():
     assert sm["n"] == 3 and sm["speedup_total"] == 20.0 / 6.0 and sm["speedup_median"] == 4.0
     assert (sm["warm_fewer_steps"], sm["warm_more_steps"]) == (1, 1)
     assert sm["k_err_warm_f16_vs_f64_max"] == 1e-5 and sm["k_err_rest_f32_vs_f64_max"] is None
+
+
+def test_run_to_convergence_jsonl_log(tmp_path):
+    """The logged convergence loop (host side) on a stand-in lattice whose Darcy
+    velocity approaches 1e-3 geometrically: one JSON line per check, the stop
+    rule of lbm_run_to_convergence (|dv| <= tol |v| between checks), and the
+    same permeability formula."""
+    import json
+    from types import SimpleNamespace
+    from taichi_lbm3d_gb300 import LB3D_Solver_Single_Phase
+
+    class FakeLattice:
+        def __init__(self):
+            self.steps = 0
+
+        def step(self, n):
+            self.steps += n
+
+        def stats(self):
+            vm = 1e-3 * (1 - 0.5 ** (self.steps / 100))
+            return SimpleNamespace(mom=(vm * 64, 0.0, 0.0), mass=40.0, max_v=2 * vm, n_nonfinite=0)
+
+        def info(self):
+            return SimpleNamespace(n_fluid=40)
+
+    lb = LB3D_Solver_Single_Phase(4, 4, 4, viscosity_convention="standard", guo_convention="standard")
+    lb.niu, lb.fx, lb.tau_f = 0.1, 1e-5, 0.8
+    lb._lat = FakeLattice()
+    path = tmp_path / "conv.jsonl"
+    r = lb.run_to_convergence(tol=1e-3, check_every=100, max_steps=10_000, log=str(path))
+    rows = [json.loads(x) for x in path.read_text().splitlines()]
+    # rel change between checks n and n+1 is 0.5^(n+1) / (1 - 0.5^(n+1)) <= 1e-3 first at n + 1 = 10
+    assert r["converged"] and r["steps"] == 1000 and len(rows) == 10
+    assert rows[0]["rel_change"] is None and rows[-1]["rel_change"] <= 1e-3 < rows[-2]["rel_change"]
+    assert abs(r["k"] - 0.1 * r["darcy_v"] / 1e-5) <= 1e-12 * r["k"]
+    assert rows[-1]["steps"] == 1000 and rows[-1]["mass"] == 40.0
