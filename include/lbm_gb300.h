@@ -243,9 +243,12 @@ int lbm_read_ascii(const char* path, double* out, int64_t n, int64_t* count);
  * (NULL = default stream) and a host LbmStats; the call allocates nothing.  Its
  * scratch is a static device array of LBM_NOALLOC_SCRATCH_BYTES that every GPU
  * loading the library holds until exit.  n above LBM_NOALLOC_MAX_NODES is
- * rejected with LBM_EINVAL.  The first call on a device looks up the scratch's
- * device address (make it before any stream capture).  Calls share the scratch:
- * calls that overlap on the GPU race and must be serialised by the caller. */
+ * rejected with LBM_EINVAL.  The call is synchronous: it waits for `stream` and
+ * returns the sums in *out.  Its first call on a device looks up the scratch's
+ * device address (make that first call before any stream capture begins); the
+ * lookup is repeated when the device's context has been re-created since (for
+ * example after cudaDeviceReset).  Calls share the scratch: calls that overlap
+ * on the GPU race and must be serialised by the caller. */
 #define LBM_NOALLOC_MAX_NODES 67108864
 #define LBM_NOALLOC_SCRATCH_BYTES 196656
 int lbm_reduce_macros_noalloc(const float* rho, const float* v, int64_t n, int64_t v_stride, void* stream,

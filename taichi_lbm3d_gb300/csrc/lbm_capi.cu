@@ -543,6 +543,8 @@ int lbm_run_to_convergence(LbmHandle* h, double tol, int32_t check_every, int64_
         LbmStats st;
         rc = red_launch(h, &st, nullptr);
         if (rc) return rc;
+        rc = sp_debug_take(h);       // -DLBM_DEBUG builds: index checks of these steps (LBM_OK otherwise)
+        if (rc) return rc;
         if (st.n_nonfinite) {
             *darcy_v = NAN;
             *steps = done;

@@ -12,15 +12,21 @@
 // static __device__ array.  Every GPU that loads this library holds it
 // (LBM_NOALLOC_SCRATCH_BYTES) until the process exits.  In host code the
 // symbol is only a host-side stand-in, never a device address, so the device
-// address is fetched with cudaGetSymbolAddress once per device, with that
-// device current, on the first call made on it (make that first call before
-// any stream capture) and cached.
+// address is fetched with cudaGetSymbolAddress, with the device current, on the
+// first call made on that device (make that first call before any stream
+// capture begins) and cached together with the unique ID of the CUDA context it
+// belongs to.  A later call that finds another context current on the device
+// (the caller ran cudaDeviceReset, or the primary context was released and
+// created again, which reloads this module and can move the array) looks the
+// address up again instead of using the stale one.  The call is synchronous:
+// it waits for its stream and returns the sums in host memory.
 //
 // Every call shares the one array and leaves its partials in it.  Each call
 // writes every slot it later reads (one per block, then the result slots), so
 // nothing has to be cleared between calls; calls that overlap on the GPU (two
 // streams, two host threads) race on the array and must be serialised by the
 // caller.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -104,24 +110,65 @@ __global__ void __launch_bounds__(NA_THREADS) na_final_kernel(double* __restrict
 }
 
 std::mutex g_na_mu;
-double* g_na_dev_ptr[64] = {};
+struct NaScratch {
+    double* ptr = nullptr;
+    unsigned long long ctx_id = 0;   // context the address belongs to
+    bool valid = false;
+};
+NaScratch g_na_dev[64];
 
-// Device address of g_noalloc_scratch on the current device (set up once per device).
+// Driver entry points, resolved through the runtime (no link against libcuda).
+typedef CUresult(CUDAAPI* NaCtxGetCurrent)(CUcontext*);
+typedef CUresult(CUDAAPI* NaCtxGetId)(CUcontext, unsigned long long*);
+NaCtxGetCurrent g_na_get_current = nullptr;
+NaCtxGetId g_na_get_id = nullptr;
+std::once_flag g_na_once;
+
+// Unique ID of the context current on this thread; false when it cannot be
+// known (no context yet, or the driver entry points are unavailable).
+bool na_context_id(unsigned long long* id) {
+    std::call_once(g_na_once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_na_get_current = (NaCtxGetCurrent)f;
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_na_get_id = (NaCtxGetId)f;
+    });
+    if (!g_na_get_current || !g_na_get_id) return false;
+    CUcontext ctx = nullptr;
+    if (g_na_get_current(&ctx) != CUDA_SUCCESS || ctx == nullptr) return false;
+    return g_na_get_id(ctx, id) == CUDA_SUCCESS;
+}
+
+// Device address of g_noalloc_scratch on the current device: looked up on the
+// first call on a device and again whenever the current context differs from
+// the one the cached address was taken in (every call, if the context ID
+// cannot be read).
 int na_scratch(double** out) {
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return lbm_set_err(nullptr, LBM_ECUDA, std::string("lbm_reduce_macros_noalloc: cudaGetDevice: ") + cudaGetErrorString(e));
     if (dev < 0 || dev >= 64) return lbm_set_err(nullptr, LBM_EINVAL, "lbm_reduce_macros_noalloc: device ordinal >= 64");
     std::lock_guard<std::mutex> lk(g_na_mu);
-    if (!g_na_dev_ptr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || p == nullptr)
-            return lbm_set_err(nullptr, LBM_ECUDA, std::string("lbm_reduce_macros_noalloc: cudaGetSymbolAddress: ") +
-                                                       cudaGetErrorString(e));
-        g_na_dev_ptr[dev] = (double*)p;
+    unsigned long long id = 0;
+    NaScratch& c = g_na_dev[dev];
+    if (c.valid && na_context_id(&id) && id == c.ctx_id) {
+        *out = c.ptr;
+        return LBM_OK;
     }
-    *out = g_na_dev_ptr[dev];
+    c.valid = false;
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);     // makes the device's primary context current if none is
+    if (e != cudaSuccess || p == nullptr)
+        return lbm_set_err(nullptr, LBM_ECUDA, std::string("lbm_reduce_macros_noalloc: cudaGetSymbolAddress: ") +
+                                                   cudaGetErrorString(e));
+    c.ptr = (double*)p;
+    c.valid = na_context_id(&c.ctx_id);
+    *out = c.ptr;
     return LBM_OK;
 }
 

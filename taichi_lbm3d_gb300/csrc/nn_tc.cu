@@ -654,7 +654,8 @@ int nn_wgrad_tc_launch(const void* in, const void* g, float* part, float* dbpart
     case C: {                                                                                                  \
         auto k = conv3d_wgrad_tc_kernel<C>;                                                                    \
         if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)    \
-            return lbm_set_err(nullptr, LBM_ECUDA, "lbm_nn_conv3d_wgrad: shared memory attribute");            \
+            return lbm_set_err(nullptr, LBM_ECUDA, "lbm_nn_conv3d_wgrad: shared memory attribute refused for " +  \
+                                                       std::to_string(smem) + " bytes");                        \
         k<<<grid, TC_THREADS, smem, s>>>((const bf16*)in, (const bf16*)g, part, dbpart, n, d, h, w, cout);     \
         break;                                                                                                 \
     }

@@ -1,9 +1,9 @@
 """Generate golden fixtures by running the reference solver's own source.
 
-Run in a container that has the reference checkout (read-only) at
-``--ref`` (default ``/root/reference``):
+Run where a checkout of the reference (taichi_LBM3D) is available, read-only,
+giving its root with ``--ref`` or the ``TAICHI_LBM3D_REF`` environment variable:
 
-    python tests/golden/make_golden.py [--ref PATH] [--only NAME ...]
+    python tests/golden/make_golden.py --ref PATH [--only NAME ...]
 
 Taichi is not installable offline, so ``taichi_numpy_shim`` stands in for it:
 the reference's kernel bodies (``Single_phase/LBM_3D_SinglePhase_Solver.py``,
@@ -392,9 +392,12 @@ def gen_grey(ref, only):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("TAICHI_LBM3D_REF"),
+                    help="root of the reference checkout (or set TAICHI_LBM3D_REF)")
     ap.add_argument("--only", nargs="*", default=[])
     a = ap.parse_args()
+    if not a.ref:
+        ap.error("give the reference checkout with --ref PATH or TAICHI_LBM3D_REF")
     gen_single_phase(a.ref, a.only)
     gen_two_phase(a.ref, a.only)
     gen_grey(a.ref, a.only)

@@ -70,6 +70,36 @@ def test_noalloc_reduction_matches_lbm_reductions_twice():
         lat.close()
 
 
+def test_noalloc_padded_stride_on_a_caller_stream():
+    """The layout real callers hand over: v components padded to a stride above
+    n (the library's own node arrays pad to 64), the padding filled with NaN so
+    that reading it would show, and a non-default stream owned by the caller."""
+    import torch
+    from taichi_lbm3d_gb300 import _native
+    fn = _fn()
+    lat = _lattice((40, 36, 28), 33)
+    ref = lat.stats()
+    d_rho, d_v, n = _node_arrays(lat)
+    stride = (n + 63) // 64 * 64 + 64
+    v_pad = torch.full((3, stride), float("nan"), dtype=torch.float32, device="cuda")
+    v_pad[:, :n] = d_v
+    rho_pad = torch.full((stride,), float("nan"), dtype=torch.float32, device="cuda")
+    rho_pad[:n] = d_rho
+    torch.cuda.synchronize()
+    s = torch.cuda.Stream()
+    for _ in range(2):
+        st = _native.LbmStats()
+        rc = fn(rho_pad.data_ptr(), v_pad.data_ptr(), n, stride, ctypes.c_void_p(s.cuda_stream), ctypes.byref(st))
+        assert rc == 0, _native.last_error()
+        assert st.n_fluid == ref.n_fluid == n
+        assert st.n_nonfinite == 0
+        assert abs(st.mass - ref.mass) <= REL * abs(ref.mass)
+        for c in range(3):
+            assert abs(st.mom[c] - ref.mom[c]) <= REL * np.abs(lat.macros()[1][..., c]).sum() + 1e-300
+        assert st.max_v == ref.max_v
+    lat.close()
+
+
 def test_noalloc_rejects_sizes_beyond_its_scratch():
     from taichi_lbm3d_gb300 import _native
     fn = _fn()
