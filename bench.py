@@ -13,7 +13,11 @@ through the public solver class with host buffers (geometry upload, init, K
 steps, rho/v download inside the timed region); ``roofline`` = algorithmic
 bytes (152 B per fluid node per step) / launch time against the measured HBM
 copy bandwidth; ``cpu_baseline`` = the CPU oracle (the reference's four-sweep
-algorithm in C/OpenMP) on a bounded sample of the same workload.
+algorithm in C/OpenMP) on a bounded sample of the same workload;
+``time_to_converged_k`` = the metric's second half: the same lattice run to a
+steady permeability (|dk/k| <= 1e-6 over 500 steps) by the plain FP32 kernel and
+by the chosen FP16 deviation storage, wall time and k error against an FP64 run
+of the same solver (skip with ``--no-convergence``).
 ``--impl reference`` times that CPU implementation alone on all host threads.
 Under torchrun (N > 1) every rank runs its own replica (the path is replicated,
 not sharded: there is no exchange step).
@@ -165,7 +169,10 @@ def run_variant(solid, storage, steps, warmup):
 
 
 def e2e_run(solid, steps):
-    """Same metric through the public class, host buffers in and out."""
+    """Same metric through the public class, host buffers in and out.  Returns
+    the MLUPS over the whole sequence and the seconds of its three phases:
+    setup (class construction, mask upload, device index build, init), steps
+    (run(K), synchronous) and readback (dense rho and v as fresh numpy arrays)."""
     from taichi_lbm3d_gb300 import LB3D_Solver_Single_Phase
     t0 = time.perf_counter()
     lb = LB3D_Solver_Single_Phase(*SHAPE)
@@ -174,16 +181,20 @@ def e2e_run(solid, steps):
     lb.set_bc_rho_x0(RHO_IN)
     lb.set_bc_rho_x1(RHO_OUT)
     lb.init_simulation()
+    t1 = time.perf_counter()
     lb.run(steps)
+    t2 = time.perf_counter()
     rho = lb.rho.to_numpy()
     v = lb.v.to_numpy()
-    secs = time.perf_counter() - t0
+    t3 = time.perf_counter()
     nf = lb.n_fluid
     lb.close()
     h2d = solid.size * 1                                         # the int8 mask (index built on the device)
     d2h = 16 * solid.size                                        # dense rho + v (scattered on the device)
     assert np.isfinite(rho).all() and np.isfinite(v).all()
-    return nf * steps / secs / 1e6, h2d / steps, d2h / steps
+    phases = {"setup_s": t1 - t0, "steps_s": t2 - t1, "readback_s": t3 - t2,
+              "steps_only_mlups": nf * steps / (t2 - t1) / 1e6}
+    return nf * steps / (t3 - t0) / 1e6, h2d / steps, d2h / steps, phases
 
 
 def cpu_baseline(solid, max_seconds=20.0):
@@ -207,12 +218,13 @@ def cpu_baseline(solid, max_seconds=20.0):
 
 
 def convergence(storages=("f64", "f32", "f32dev", "f16", "bf16"), tol=1e-6, check_every=500, max_steps=200_000,
-                shape=SHAPE, visc="standard"):
+                shape=SHAPE, visc="standard", solid=None):
     """The 256^3 pack run to steady state: |dk/k| <= tol over check_every steps.
     Each storage variant reports steps, wall time and its permeability error
     against the FP64 run of the same solver."""
     from taichi_lbm3d_gb300 import LB3D_Solver_Single_Phase
-    solid = geometry() if shape == SHAPE else None
+    if solid is None and shape == SHAPE:
+        solid = geometry()
     if solid is None:
         from taichi_lbm3d_gb300.geometry import sphere_pack
         solid = sphere_pack(shape, PACK["rmin"], PACK["rmax"], PACK["porosity"], PACK["seed"])
@@ -234,6 +246,27 @@ def convergence(storages=("f64", "f32", "f32dev", "f16", "bf16"), tol=1e-6, chec
         k64 = out["f64"]["k"]
         for sto, r in out.items():
             r["k_rel_err_vs_f64"] = abs(r["k"] - k64) / abs(k64)
+    return out
+
+
+CHOSEN_STORAGE = "f16"      # the mixed-precision storage the method uses (FP16 deviations, FP32 collide)
+
+
+def converged_k_summary(res, tol=1e-6, check_every=500):
+    """The metric's second half: wall time to the converged permeability of
+    the plain FP32 kernel (reference arithmetic) and of the chosen storage, each
+    with its k error against the FP64 run of the same solver."""
+    def one(r):
+        return {"steps": int(r["steps"]), "seconds": r["seconds"], "mlups": r["mlups"], "k": r["k"],
+                "converged": bool(r["converged"]), "k_rel_err_vs_f64": r.get("k_rel_err_vs_f64")}
+    out = {"criterion": "|dk/k| <= %g over %d steps" % (tol, check_every),
+           "conventions": "standard (tau = 3 niu + 1/2, Guo 3/9), same lattice, faces and niu as the step",
+           "accuracy_bar": 1e-3, "f64": one(res["f64"]), "plain_f32": one(res["f32"]),
+           "chosen": dict(one(res[CHOSEN_STORAGE]), storage=CHOSEN_STORAGE)}
+    out["others"] = {k: one(v) for k, v in res.items() if k not in ("f64", "f32", CHOSEN_STORAGE)}
+    out["chosen_speedup_wall"] = res["f32"]["seconds"] / res[CHOSEN_STORAGE]["seconds"]
+    out["plain_within_bar"] = res["f32"]["k_rel_err_vs_f64"] <= 1e-3
+    out["chosen_within_bar"] = res[CHOSEN_STORAGE]["k_rel_err_vs_f64"] <= 1e-3
     return out
 
 
@@ -481,7 +514,8 @@ def grey_field(shape=SHAPE):
     the spheres and a grey layer ns = 0.25 on pore cells within 1.5 cells of a
     sphere (unresolved roughness), ns = 0 elsewhere."""
     from taichi_lbm3d_gb300.geometry import distance_to_solid
-    solid = geometry() if shape == SHAPE else None
+    if solid is None and shape == SHAPE:
+        solid = geometry()
     if solid is None:
         from taichi_lbm3d_gb300.geometry import sphere_pack
         solid = sphere_pack(shape, PACK["rmin"], PACK["rmax"], PACK["porosity"], PACK["seed"])
@@ -592,6 +626,8 @@ def main():
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--no-convergence", action="store_true",
+                    help="skip the time-to-converged-k legs (FP64, FP32, FP16, ...) of the default line")
     ap.add_argument("--convergence", action="store_true",
                     help="run the 256^3 pack to steady state in FP64/FP32/FP16/BF16 and print k errors")
     ap.add_argument("--batched", action="store_true",
@@ -640,11 +676,13 @@ def main():
         if rank != 0:
             return 0
         solid = geometry()
+        nf = int((solid == 0).sum())
         cb = cpu_baseline(solid, max_seconds=min(120.0, 3.0 * max(1, a.steps)))
         line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": a.gpus,
                 "steps": int(re.match(r"(\d+)", cb["sample"]).group(1)), "warmup": 1,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-                "data": "synthetic (seeded sphere pack)", "config": workload_config(),
+                "data": "synthetic (seeded sphere pack, numpy default_rng seed 2)",
+                "config": dict(workload_config(), n_fluid=nf, porosity_after_percolation=float(nf) / solid.size),
                 "cpu_baseline": cb,
                 "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
                 "note": "the reference's Taichi ti.cpu path is not installable offline; this is the C oracle "
@@ -723,12 +761,14 @@ def main():
                 var[sto] = {"value": nfv * min(a.steps, 1000) / sv / 1e6, "unit": UNIT,
                             "gbs_algorithmic": BYTES_PER_NODE[sto] * nfv * min(a.steps, 1000) / sv / 1e9}
             line["variants"] = var
-        e2e, h2d, d2h = e2e_run(solid, a.steps)
+        e2e, h2d, d2h, phases = e2e_run(solid, a.steps)
         line["e2e"] = {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                        "path": "LB3D_Solver_Single_Phase: solid.from_numpy, init_simulation, run(K), "
-                               "rho/v to_numpy, host wall clock"}
+                               "rho/v to_numpy, host wall clock", "phases": phases}
         if not a.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(solid)
+        if not a.no_convergence:
+            line["time_to_converged_k"] = converged_k_summary(convergence(solid=solid))
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
