@@ -106,6 +106,11 @@ void dev_free(T*& p) {
 void free_lattice(LbmHandle* h) {
     dev_free(h->d_map);
     dev_free(h->d_coord);
+    dev_free(h->d_tinfo);
+    h->d_spt_ctr = nullptr;
+    h->spt_base = 0;
+    h->ntile = 0;
+    h->tiled = false;
     dev_free(h->d_f[0]);
     dev_free(h->d_f[1]);
     dev_free(h->d_vprev);
@@ -255,6 +260,7 @@ int lbm_set_geometry_strided(LbmHandle* h, const int8_t* solid, int64_t si, int6
     free_lattice(h);
     h->have_geometry = h->initialized = h->macros_valid = false;
     int rc = geom_build(h, solid, si, sj, sk);
+    if (!rc) rc = sp_tiles_setup(h);
     if (rc) { free_lattice(h); return rc; }
     const size_t rbytes = h->f64 ? 8 : 4;
     rc = rc ? rc : dev_alloc(h, &h->d_f[0], h->elem * 19 * h->np, "f_A");

@@ -169,8 +169,13 @@ int geom_build(LbmHandle* h, const int8_t* solid, int64_t si, int64_t sj, int64_
     if (!rc) {
         h->n_fluid = (int32_t)total;
         h->np = (std::max<int64_t>(total, 1) + 63) / 64 * 64;
-        rc = lbm_cuda_check(h, cudaMalloc((void**)&h->d_map, sizeof(int32_t) * ncell), "map");
-        if (!rc) h->device_bytes += sizeof(int32_t) * ncell;
+        // LBM_MAP_PAD entries of -1 after the last cell: the step kernel stages map
+        // rows with 16-byte bulk copies, which may round a row block up past its end
+        rc = lbm_cuda_check(h, cudaMalloc((void**)&h->d_map, sizeof(int32_t) * (ncell + LBM_MAP_PAD)), "map");
+        if (!rc) h->device_bytes += sizeof(int32_t) * (ncell + LBM_MAP_PAD);
+        if (!rc)
+            rc = lbm_cuda_check(h, cudaMemsetAsync(h->d_map + ncell, 0xff, sizeof(int32_t) * LBM_MAP_PAD, st),
+                                "map padding");
         if (!rc) rc = lbm_cuda_check(h, cudaMalloc((void**)&h->d_coord, sizeof(uint32_t) * h->np), "coord");
         if (!rc) h->device_bytes += sizeof(uint32_t) * h->np;
         if (!rc) rc = lbm_cuda_check(h, cudaMemsetAsync(h->d_coord, 0, sizeof(uint32_t) * h->np, st), "clear coord");

@@ -42,6 +42,9 @@ struct SpConsts {
     R gc, gd;
 };
 
+// int32 entries of -1 allocated after the dense map's last cell (bulk-copy rounding).
+#define LBM_MAP_PAD 16
+
 struct LbmHandle {
     LbmParams p{};
     int device = 0;
@@ -63,7 +66,13 @@ struct LbmHandle {
     bool l2_persist = false;               // the map is this stream's persisting L2 window
     std::vector<float> psi0;               // dense initial psi (two phase)
 
-    int32_t* d_map = nullptr;              // dense: node index or -1 (solid)
+    int32_t* d_map = nullptr;              // dense: node index or -1 (solid); LBM_MAP_PAD extra -1 entries
+    int2* d_tinfo = nullptr;               // staged step: per 256-node tile, first staged row and plane/rows
+    int32_t ntile = 0;
+    bool tiled = false;                    // single-phase steps use a staged kernel
+    int tiled_mode = 0;                    // 1: persistent staged kernel, 2: one tile per CTA
+    unsigned long long* d_spt_ctr = nullptr;  // its tile claim counter (inside the d_tinfo allocation)
+    unsigned long long spt_base = 0;       // counter value at the next launch's first claim
     uint32_t* d_coord = nullptr;           // packed (i,j,k) per node
     void* d_f[2] = {nullptr, nullptr};     // populations, 19 x np elements in AoSoA-32 chunks
     int cur = 0;
@@ -102,6 +111,7 @@ int geom_dense_out(LbmHandle* h, const void* dsrc, int comps, O* out, O fill);
 int sp_launch_init(LbmHandle* h, const void* rho_nodes, const void* v_nodes);
 int sp_launch_steps(LbmHandle* h, int32_t n, bool macros_last);
 int sp_launch_debug_stream(LbmHandle* h, const float* d_in, float* d_out);
+int sp_tiles_setup(LbmHandle* h);
 template <typename R>
 SpConsts<R> sp_make_consts(const LbmHandle* h);
 
