@@ -63,7 +63,10 @@ struct LbmBatch {
     cudaGraphExec_t graph = nullptr;
     int32_t graph_steps = 0;
     std::vector<int64_t> steps;         // per subvolume
+    uint32_t seed_step = 0;             // steps taken since init (16-bit rounding seed)
 };
+
+static const uint32_t* seed_base(const LbmBatch* b) { return reinterpret_cast<const uint32_t*>(b->d_counters + 4096); }
 
 namespace {
 using namespace lbmk;
@@ -77,8 +80,8 @@ __global__ void __launch_bounds__(256, STORE == LBM_STORE_F64 ? 1 : 4) batch_ste
                                                          typename Codec<STORE>::T* __restrict__ fout,
                                                          const int32_t* __restrict__ map,
                                                          const uint32_t* __restrict__ coord,
-                                                         const float* __restrict__ rref_in,
-                                                         float* __restrict__ rref_out, double* __restrict__ partial) {
+                                                         const uint32_t* __restrict__ seed_base,
+                                                         double* __restrict__ partial) {
     using Cd = Codec<STORE>;
     using R = typename Cd::R;
     __shared__ int s_tile;
@@ -96,14 +99,16 @@ __global__ void __launch_bounds__(256, STORE == LBM_STORE_F64 ? 1 : 4) batch_ste
         const typename Cd::T* sfin = sub_pop(fin, sd.node_begin);
         typename Cd::T* sfout = sub_pop(fout, sd.node_begin);
         const uint32_t* scoord = coord + sd.node_begin;
-        const float* srin = sub_node(rref_in, sd.node_begin);
-        float* srout = sub_node(rref_out, sd.node_begin);
+        // 16-bit codecs: all faces periodic, so the reference density is 0; the
+        // rounding bits are those of a single lattice at the same step (step
+        // index = the launch group's first step, set before the group, + k)
+        const uint32_t seed = *seed_base + C.seed;
         double acc = 0.0;
         for (int n = tl.begin + threadIdx.x; n < tl.end; n += blockDim.x) {
             const uint32_t pc = __ldg(scoord + n);
             const int i = lbm_pi(pc), j = lbm_pj(pc), k = lbm_pk(pc);
             R F[19];
-            gather_node<STORE>(F, sfin, smap, n, sd.nx, sd.ny, sd.nz, i, j, k, srin);
+            gather_node<STORE>(F, sfin, smap, n, sd.nx, sd.ny, sd.nz, i, j, k);
             R r = F[0];
 #pragma unroll
             for (int s = 1; s < 19; ++s) r = r + F[s];
@@ -116,7 +121,7 @@ __global__ void __launch_bounds__(256, STORE == LBM_STORE_F64 ? 1 : 4) batch_ste
             }
             if constexpr (CHECK) acc += (double)vx;
             collide_sp<R, FORCE, Cd::DEV>(F, r, vx, vy, vz, C);
-            store_node<STORE>(F, sfout, n, r, srout);
+            store_node<STORE>(F, sfout, n, (R)0, seed);
         }
         if constexpr (CHECK) {
             for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
@@ -137,8 +142,7 @@ __global__ void __launch_bounds__(256, STORE == LBM_STORE_F64 ? 1 : 4) batch_ste
 template <int STORE, bool FORCE>
 __global__ void batch_macros_kernel(const __grid_constant__ SpConsts<typename Codec<STORE>::R> C, BatchSub sd,
                                     const typename Codec<STORE>::T* __restrict__ fin, const int32_t* __restrict__ map,
-                                    const uint32_t* __restrict__ coord, const float* __restrict__ rref_in,
-                                    float* __restrict__ out) {
+                                    const uint32_t* __restrict__ coord, float* __restrict__ out) {
     using Cd = Codec<STORE>;
     using R = typename Cd::R;
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
@@ -146,7 +150,7 @@ __global__ void batch_macros_kernel(const __grid_constant__ SpConsts<typename Co
     const uint32_t pc = __ldg(coord + sd.node_begin + a);
     R F[19];
     gather_node<STORE>(F, sub_pop(fin, sd.node_begin), map + sd.map_off, a, sd.nx, sd.ny, sd.nz, lbm_pi(pc), lbm_pj(pc),
-                       lbm_pk(pc), sub_node(rref_in, sd.node_begin));
+                       lbm_pk(pc));
     R r = F[0];
 #pragma unroll
     for (int s = 1; s < 19; ++s) r = r + F[s];
@@ -166,7 +170,7 @@ __global__ void batch_macros_kernel(const __grid_constant__ SpConsts<typename Co
 template <int STORE, bool FORCE>
 __global__ void batch_init_kernel(const __grid_constant__ SpConsts<typename Codec<STORE>::R> C,
                                   typename Codec<STORE>::T* __restrict__ fout, const BatchSub* __restrict__ subs,
-                                  int n_sub, float* __restrict__ rref_out) {
+                                  int n_sub) {
     using Cd = Codec<STORE>;
     using R = typename Cd::R;
     if (blockIdx.y >= (unsigned)n_sub) return;
@@ -178,7 +182,7 @@ __global__ void batch_init_kernel(const __grid_constant__ SpConsts<typename Code
     else lbm_feq_all<R>((R)1, (R)0, (R)0, (R)0, F);
     const R r = Cd::DEV ? (R)0 : (R)1;
     collide_sp<R, FORCE, Cd::DEV>(F, r, (R)0, (R)0, (R)0, C);
-    store_node<STORE>(F, sub_pop(fout, sd.node_begin), n, r, sub_node(rref_out, sd.node_begin));
+    store_node<STORE>(F, sub_pop(fout, sd.node_begin), n, (R)0, ~0u);   // as the single-lattice init
 }
 
 int batch_err(LbmBatch* b, int code, const std::string& m) { return lbm_set_err(&b->h, code, m); }
@@ -189,14 +193,15 @@ int launch_one(LbmBatch* b, int k, bool check, cudaStream_t s) {
     using T = typename Cd::T;
     using R = typename Cd::R;
     LbmHandle* h = &b->h;
-    const SpConsts<R> C = sp_make_consts<R>(h);
+    SpConsts<R> C = sp_make_consts<R>(h);
+    C.seed = (uint32_t)k;   // step within the launch group; the group's first step is read on the device
     const int cur = k & 1;
     const T* fin = (const T*)h->d_f[cur];
     T* fout = (T*)h->d_f[cur ^ 1];
     int32_t* ctr = b->d_counters + k;
     auto args = [&](auto kern) {
         kern<<<b->grid, b->block, 0, s>>>(C, b->d_subs, b->d_tiles, b->d_ntiles, ctr, fin, fout, h->d_map, h->d_coord,
-                                          h->d_rref[cur], h->d_rref[cur ^ 1], b->d_partial);
+                                          seed_base(b), b->d_partial);
     };
     if (h->force) {
         if (check) args(batch_step_kernel<STORE, true, true>);
@@ -248,7 +253,7 @@ int init_t(LbmBatch* b) {
     for (auto& s : b->subs) maxn = std::max(maxn, s.n_fluid);
     dim3 grid((maxn + 255) / 256, (unsigned)b->subs.size());
     auto k = h->force ? batch_init_kernel<STORE, true> : batch_init_kernel<STORE, false>;
-    k<<<grid, 256, 0, h->stream>>>(C, (typename Cd::T*)h->d_f[0], b->d_subs, (int)b->subs.size(), h->d_rref[0]);
+    k<<<grid, 256, 0, h->stream>>>(C, (typename Cd::T*)h->d_f[0], b->d_subs, (int)b->subs.size());
     return lbm_cuda_check(h, cudaGetLastError(), "batch_init_kernel launch");
 }
 
@@ -262,7 +267,7 @@ int macros_t(LbmBatch* b, int q, float* d_out) {
     const int grid = (sd.n_fluid + 255) / 256;
     auto k = h->force ? batch_macros_kernel<STORE, true> : batch_macros_kernel<STORE, false>;
     if (grid > 0)
-        k<<<grid, 256, 0, h->stream>>>(C, sd, (const typename Cd::T*)h->d_f[0], h->d_map, h->d_coord, h->d_rref[0], d_out);
+        k<<<grid, 256, 0, h->stream>>>(C, sd, (const typename Cd::T*)h->d_f[0], h->d_map, h->d_coord, d_out);
     return lbm_cuda_check(h, cudaGetLastError(), "batch_macros_kernel launch");
 }
 
@@ -376,7 +381,6 @@ int lbm_batch_create(const LbmParams* params, int32_t n_sub, const int32_t* dims
     b->steps.assign(n_sub, 0);
     b->max_tiles = 0;
     for (auto& s : b->subs) b->max_tiles += (s.n_fluid + 31) / 32;   // tiles of >= 32 nodes
-    const bool rhoref = p.storage == LBM_STORE_F16_DEV || p.storage == LBM_STORE_BF16_DEV;
     auto alloc = [&](void** ptr, size_t bytes) {
         if (rc) return;
         if (cudaMalloc(ptr, bytes ? bytes : 16) != cudaSuccess) rc = lbm_set_err(nullptr, LBM_ENOMEM, "lbm_batch_create: out of device memory");
@@ -386,15 +390,11 @@ int lbm_batch_create(const LbmParams* params, int32_t n_sub, const int32_t* dims
     alloc((void**)&h->d_coord, sizeof(uint32_t) * h->np);
     alloc(&h->d_f[0], h->elem * 19 * h->np);
     alloc(&h->d_f[1], h->elem * 19 * h->np);
-    if (rhoref) {
-        alloc((void**)&h->d_rref[0], sizeof(float) * h->np);
-        alloc((void**)&h->d_rref[1], sizeof(float) * h->np);
-    }
     alloc((void**)&b->d_subs, sizeof(BatchSub) * n_sub);
     alloc((void**)&b->d_tiles, sizeof(BatchTile) * b->max_tiles);
     alloc((void**)&b->d_ntiles, sizeof(int32_t));
     alloc((void**)&b->d_partial, sizeof(double) * b->max_tiles);
-    alloc((void**)&b->d_counters, sizeof(int32_t) * 4096);
+    alloc((void**)&b->d_counters, sizeof(int32_t) * (4096 + 4));   // + the first step of the launch group
     if (!rc) rc = lbm_cuda_check(h, cudaMemcpy(h->d_map, map.data(), sizeof(int32_t) * map.size(), cudaMemcpyHostToDevice), "copy map");
     if (!rc) rc = lbm_cuda_check(h, cudaMemcpy(h->d_coord, coord.data(), sizeof(uint32_t) * h->np, cudaMemcpyHostToDevice), "copy coord");
     if (!rc) rc = lbm_cuda_check(h, cudaMemcpy(b->d_subs, b->subs.data(), sizeof(BatchSub) * n_sub, cudaMemcpyHostToDevice), "copy subs");
@@ -419,8 +419,6 @@ int lbm_batch_destroy(LbmBatch* b) {
     cudaFree(h->d_coord);
     cudaFree(h->d_f[0]);
     cudaFree(h->d_f[1]);
-    cudaFree(h->d_rref[0]);
-    cudaFree(h->d_rref[1]);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete b;
     return LBM_OK;
@@ -458,8 +456,18 @@ int lbm_batch_init(LbmBatch* b) {
     default: rc = batch_err(b, LBM_EINVAL, "unknown storage");
     }
     if (!rc) rc = rebuild_tiles(b);
+    b->seed_step = 0;
     destroy_graph(b);
     return rc;
+}
+
+// Step index of the next launch group's first step (rounding seed), written to
+// the device before the group; advanced by the group's steps.
+static int set_seed_base(LbmBatch* b, int32_t chunk) {
+    const uint32_t v = b->seed_step;
+    b->seed_step += (uint32_t)chunk;
+    return lbm_cuda_check(&b->h, cudaMemcpyAsync(b->d_counters + 4096, &v, sizeof(v), cudaMemcpyHostToDevice, b->h.stream),
+                          "seed base");
 }
 
 // Run `nsteps` (even) steps of all active subvolumes: graph launches of
@@ -473,13 +481,15 @@ static int batch_run(LbmBatch* b, int32_t nsteps, int32_t chunk, int32_t use_gra
             if (rc) return rc;
         }
         for (int32_t done = 0; done < nsteps; done += chunk) {
-            int rc = lbm_cuda_check(h, cudaGraphLaunch(b->graph, h->stream), "graph launch");
+            int rc = set_seed_base(b, chunk);
+            if (!rc) rc = lbm_cuda_check(h, cudaGraphLaunch(b->graph, h->stream), "graph launch");
             if (rc) return rc;
         }
         return LBM_OK;
     }
     for (int32_t done = 0; done < nsteps; done += chunk) {
-        int rc = lbm_cuda_check(h, cudaMemsetAsync(b->d_counters, 0, sizeof(int32_t) * chunk, h->stream), "counters");
+        int rc = set_seed_base(b, chunk);
+        if (!rc) rc = lbm_cuda_check(h, cudaMemsetAsync(b->d_counters, 0, sizeof(int32_t) * chunk, h->stream), "counters");
         for (int k = 0; k < chunk && !rc; ++k) rc = launch_dispatch(b, k, k == chunk - 1, h->stream);
         if (rc) return rc;
     }

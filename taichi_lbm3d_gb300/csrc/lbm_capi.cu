@@ -116,8 +116,6 @@ void free_lattice(LbmHandle* h) {
     dev_free(h->d_vprev);
     dev_free(h->d_rho);
     dev_free(h->d_v);
-    dev_free(h->d_rref[0]);
-    dev_free(h->d_rref[1]);
     dev_free(h->d_psi);
     dev_free(h->d_rr[0]);
     dev_free(h->d_rr[1]);
@@ -268,10 +266,6 @@ int lbm_set_geometry_strided(LbmHandle* h, const int8_t* solid, int64_t si, int6
     rc = rc ? rc : dev_alloc(h, &h->d_vprev, rbytes * 3 * h->np, "vprev");
     rc = rc ? rc : dev_alloc(h, &h->d_rho, rbytes * h->np, "rho");
     rc = rc ? rc : dev_alloc(h, &h->d_v, rbytes * 3 * h->np, "v");
-    if (h->p.storage == LBM_STORE_F16_DEV || h->p.storage == LBM_STORE_BF16_DEV) {
-        rc = rc ? rc : dev_alloc(h, &h->d_rref[0], sizeof(float) * h->np, "node density A");
-        rc = rc ? rc : dev_alloc(h, &h->d_rref[1], sizeof(float) * h->np, "node density B");
-    }
     if (!rc && h->p.two_phase) {
         rc = rc ? rc : dev_alloc(h, &h->d_psi, rbytes * h->np, "psi");
         rc = rc ? rc : dev_alloc(h, &h->d_rr[0], rbytes * h->np, "rho_r A");
@@ -621,6 +615,20 @@ int lbm_get_neighbors(LbmHandle* h, int32_t* src) {
     return LBM_OK;
 }
 
+// Reference density of the 16-bit codecs per fluid node (the device's FP32
+// rho'_ref = a + b i at the node's x), empty for the other storages.
+static int host_ref_density(LbmHandle* h, std::vector<float>& rr) {
+    rr.clear();
+    if (h->p.storage != LBM_STORE_F16_DEV && h->p.storage != LBM_STORE_BF16_DEV) return LBM_OK;
+    int rc = geom_host_index(h);
+    if (rc) return rc;
+    const SpConsts<float> C = sp_make_consts<float>(h);
+    rr.resize(h->np, 0.0f);
+    for (int32_t n = 0; n < h->n_fluid; ++n)
+        rr[n] = std::fmaf(C.ref_b, (float)(h->cell_of_node[n] % h->p.nx), C.ref_a);
+    return LBM_OK;
+}
+
 int lbm_get_populations(LbmHandle* h, double* f) {
     if (!h || !f) return lbm_set_err(h, LBM_EINVAL, "lbm_get_populations: NULL argument");
     if (!h->initialized || h->p.two_phase) return lbm_set_err(h, LBM_ESTATE, "lbm_get_populations: needs an initialised single-phase handle");
@@ -628,11 +636,8 @@ int lbm_get_populations(LbmHandle* h, double* f) {
     int rc = lbm_cuda_check(h, cudaMemcpy(tmp.data(), h->d_f[h->cur], tmp.size(), cudaMemcpyDeviceToHost), "copy f");
     if (rc) return rc;
     std::vector<float> rr;
-    if (h->d_rref[h->cur]) {
-        rr.resize(h->np);
-        rc = lbm_cuda_check(h, cudaMemcpy(rr.data(), h->d_rref[h->cur], sizeof(float) * h->np, cudaMemcpyDeviceToHost), "copy rho'");
-        if (rc) return rc;
-    }
+    rc = host_ref_density(h, rr);
+    if (rc) return rc;
     for (int s = 0; s < 19; ++s)
         for (int32_t n = 0; n < h->n_fluid; ++n) {
             const int64_t idx = lbm_pidx(n, s);
@@ -657,17 +662,14 @@ int lbm_set_populations(LbmHandle* h, const double* f) {
     if (!h || !f) return lbm_set_err(h, LBM_EINVAL, "lbm_set_populations: NULL argument");
     if (!h->initialized || h->p.two_phase) return lbm_set_err(h, LBM_ESTATE, "lbm_set_populations: needs an initialised single-phase handle");
     std::vector<unsigned char> tmp(h->elem * 19 * h->np, 0);
-    std::vector<float> rr(h->np, 0.0f);
-    for (int32_t n = 0; n < h->n_fluid; ++n) {   // node density for the RHOREF encodings
-        double r = 0;
-        for (int s = 0; s < 19; ++s) r += f[(int64_t)s * h->n_fluid + n];
-        rr[n] = (float)(r - 1.0);
-    }
+    std::vector<float> rr;
+    int rc = host_ref_density(h, rr);
+    if (rc) return rc;
     for (int s = 0; s < 19; ++s)
         for (int32_t n = 0; n < h->n_fluid; ++n) {
             const int64_t idx = lbm_pidx(n, s);
             const double val = f[(int64_t)s * h->n_fluid + n];
-            const double g = val - lbm_w(s) * (1.0 + (double)rr[n]);
+            const double g = rr.empty() ? 0.0 : val - lbm_w(s) * (1.0 + (double)rr[n]);   // 16-bit codecs only
             switch (h->p.storage) {
             case LBM_STORE_F32: ((float*)tmp.data())[idx] = (float)val; break;
             case LBM_STORE_F64: ((double*)tmp.data())[idx] = val; break;
@@ -676,9 +678,7 @@ int lbm_set_populations(LbmHandle* h, const double* f) {
             case LBM_STORE_BF16_DEV: ((__nv_bfloat16*)tmp.data())[idx] = __float2bfloat16_rn((float)g); break;
             }
         }
-    int rc = lbm_cuda_check(h, cudaMemcpy(h->d_f[h->cur], tmp.data(), tmp.size(), cudaMemcpyHostToDevice), "copy f");
-    if (!rc && h->d_rref[h->cur])
-        rc = lbm_cuda_check(h, cudaMemcpy(h->d_rref[h->cur], rr.data(), sizeof(float) * h->np, cudaMemcpyHostToDevice), "copy rho'");
+    rc = lbm_cuda_check(h, cudaMemcpy(h->d_f[h->cur], tmp.data(), tmp.size(), cudaMemcpyHostToDevice), "copy f");
     h->macros_valid = false;
     return rc;
 }

@@ -111,11 +111,49 @@ __device__ __forceinline__ void lbm_feq_all(R rho, R u0, R u1, R u2, R* out) {
 // f' = f - w and rho' = rho - 1 (the transforms are linear and M w is the unit
 // vector of moment 0, so only moment 0 and the macroscopic density change),
 // which keeps the small flow signal out of the rounding of f ~ w.  RHOREF
-// codecs store each node's post-collision populations relative to its own
-// density, g = f' - w rho'_node, with rho'_node kept per node in FP32; the
-// reader adds w rho'_source back.  What is left in g is the velocity and
-// non-equilibrium part, which 16-bit storage can resolve (FP16 scaled by 2^16:
-// |g| from ~1e-9 to 1 keeps 11 significant bits).
+// codecs (16-bit) store g = f' - w rho'_ref(x) with a fixed reference density
+// rho'_ref that every reader can compute from the cell's x coordinate (LbmRef:
+// the linear profile between two fixed-pressure x faces, else 0), so what is
+// left in g is the local density departure, the velocity and non-equilibrium
+// part, which 16-bit storage can resolve (FP16 scaled by 2^16: |g| from ~1e-9
+// to 1 keeps 11 significant bits) without any per-node side array.
+//
+// Encoding rounds stochastically (LBM_SR = 1, the default): random bits below
+// the kept mantissa are added to the FP32 pattern before it is truncated, so a
+// stored value is unbiased.  Rounding to nearest stalls slow steady flows, whose
+// per-step change of a population is a few 16-bit ulps (a 16-cell channel
+// stalled 3.8% off the parabola in FP16, 31% in BF16).  The random bits come
+// from a hash of (node, step), one 32-bit word per node and a multiplicative
+// spread per direction, so runs are deterministic.
+#ifndef LBM_SR
+#define LBM_SR 1
+#endif
+
+template <typename R>
+struct LbmRef {
+    R a = (R)0, b = (R)0;   // rho'_ref(i) = a + b i
+};
+template <typename R>
+__device__ __forceinline__ R lbm_ref_at(const LbmRef<R>& r, int i) {
+    return lbm_fma<R>(r.b, (R)i, r.a);
+}
+
+// 32 random bits per (node, step) (a xor-multiply avalanche of both).
+__device__ __forceinline__ uint32_t lbm_sr_hash(uint32_t n, uint32_t seed) {
+    uint32_t x = n * 0x9E3779B1u ^ (seed * 0x85EBCA77u + 0x632BE5ABu);
+    x ^= x >> 16;
+    x *= 0x7FEB352Du;
+    x ^= x >> 15;
+    x *= 0x846CA68Bu;
+    x ^= x >> 16;
+    return x;
+}
+// Direction S's bits: an odd multiplier per direction, top bits kept.
+template <int S>
+__device__ __forceinline__ uint32_t lbm_sr_bits(uint32_t h) {
+    return h * (0x2545F491u + 2u * 0x9E37u * (uint32_t)S);
+}
+
 template <int STORE> struct Codec;
 template <> struct Codec<LBM_STORE_F32> {
     using T = float; using R = float;
@@ -140,12 +178,22 @@ template <> struct Codec<LBM_STORE_F16_DEV> {
     static constexpr bool DEV = true, RHOREF = true;
     template <int S> static __device__ __forceinline__ R dec(T x) { return __half2float(x) * (1.0f / 65536.0f); }
     template <int S> static __device__ __forceinline__ T enc(R g) { return __float2half_rn(g * 65536.0f); }
+    // 13 bits below the FP16 mantissa (exact for FP16 normals; FP16
+    // subnormals, |g| < 1e-9, keep a bias below one of their ulps)
+    template <int S> static __device__ __forceinline__ T enc_sr(R g, uint32_t h) {
+        const uint32_t u = __float_as_uint(g * 65536.0f) + (lbm_sr_bits<S>(h) >> 19);
+        return __float2half_rz(__uint_as_float(u));
+    }
 };
 template <> struct Codec<LBM_STORE_BF16_DEV> {
     using T = __nv_bfloat16; using R = float;
     static constexpr bool DEV = true, RHOREF = true;
     template <int S> static __device__ __forceinline__ R dec(T x) { return __bfloat162float(x); }
     template <int S> static __device__ __forceinline__ T enc(R g) { return __float2bfloat16_rn(g); }
+    template <int S> static __device__ __forceinline__ T enc_sr(R g, uint32_t h) {
+        const uint32_t u = __float_as_uint(g) + (lbm_sr_bits<S>(h) >> 16);
+        return __float2bfloat16_rz(__uint_as_float(u));
+    }
 };
 
 // feq_S(rho, u) - w_S with rho = 1 + rho' (deviation form of lbm_feq).

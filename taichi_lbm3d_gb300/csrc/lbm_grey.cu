@@ -43,12 +43,19 @@ struct GreyGather {
     template <int S>
     static __device__ __forceinline__ void one(R* F, const R* Fo, const T* __restrict__ fin,
                                                const int32_t* __restrict__ map, const NS* __restrict__ ns,
-                                               const Rows& rows, int i, int xm, int xp,
-                                               const float* __restrict__ rref) {
+                                               const Rows& rows, int i, int xm, int xp, const RefX<R>& rx) {
         const int src = pull_source<S, XWRAP>(map, rows, i, xm, xp);
         if (src >= 0) {
             R a = Cd::template dec<S>(fin[lbm_eoff32(src) + 32 * S]);
-            if constexpr (Cd::RHOREF) a = lbm_fma<R>((R)lbm_w(S), (R)rref[src], a);
+            if constexpr (Cd::RHOREF) {
+                R rs = rx.ri;
+                if constexpr (lbm_ex(S) != 0) {
+                    const int xs = lbm_ex(S) > 0 ? xm : xp;
+                    if constexpr (XWRAP) rs = lbm_fma<R>(rx.b, (R)xs, rx.a);
+                    else rs = lbm_ex(S) > 0 ? rx.ri - rx.b : rx.ri + rx.b;
+                }
+                a = lbm_fma<R>((R)lbm_w(S), rs, a);
+            }
             F[S] = a + __ldg(ns + src) * (Fo[lbm_lr(S)] - a);
         } else {
             F[S] = grey_rest<S, R, Cd::DEV>();
@@ -60,7 +67,8 @@ template <int STORE>
 __device__ __forceinline__ void grey_gather_node(typename Codec<STORE>::R* F, const typename Codec<STORE>::T* __restrict__ fin,
                                                  const int32_t* __restrict__ map,
                                                  const typename Codec<STORE>::R* __restrict__ ns, int n, int nx, int ny,
-                                                 int nz, int i, int j, int k, const float* __restrict__ rref) {
+                                                 int nz, int i, int j, int k,
+                                                 const LbmRef<typename Codec<STORE>::R>& ref) {
     using Cd = Codec<STORE>;
     using R = typename Cd::R;
     const int xm = i == 0 ? nx - 1 : i - 1, xp = i == nx - 1 ? 0 : i + 1;
@@ -69,20 +77,21 @@ __device__ __forceinline__ void grey_gather_node(typename Codec<STORE>::R* F, co
     const Rows rows = make_rows(nx, ny, i, j, k, ym, yp, zm, zp);
     // the node's own post-collision populations (the partners of the mixing)
     const typename Cd::T* own = fin + lbm_eoff32(n);
+    const auto rx = ref_x<STORE>(ref, i);
     R Fo[19];
 #define LBM_OWN(S)                                                                        \
     Fo[S] = Cd::template dec<S>(own[32 * S]);                                             \
-    if constexpr (Cd::RHOREF) Fo[S] = lbm_fma<R>((R)lbm_w(S), (R)rref[n], Fo[S]);
+    if constexpr (Cd::RHOREF) Fo[S] = lbm_fma<R>((R)lbm_w(S), rx.ri, Fo[S]);
     LBM_OWN(0) LBM_ALL_DIRS(LBM_OWN)
 #undef LBM_OWN
     F[0] = Fo[0] + ns[n] * (Fo[0] - Fo[0]);
     const bool x_inside = i > 0 && i < nx - 1;
     if (__all_sync(__activemask(), x_inside)) {
-#define LBM_G(S) GreyGather<STORE, false>::template one<S>(F, Fo, fin, map, ns, rows, i, xm, xp, rref);
+#define LBM_G(S) GreyGather<STORE, false>::template one<S>(F, Fo, fin, map, ns, rows, i, xm, xp, rx);
         LBM_ALL_DIRS(LBM_G)
 #undef LBM_G
     } else {
-#define LBM_G(S) GreyGather<STORE, true>::template one<S>(F, Fo, fin, map, ns, rows, i, xm, xp, rref);
+#define LBM_G(S) GreyGather<STORE, true>::template one<S>(F, Fo, fin, map, ns, rows, i, xm, xp, rx);
         LBM_ALL_DIRS(LBM_G)
 #undef LBM_G
     }
@@ -113,7 +122,7 @@ __global__ void __launch_bounds__(256, STORE == LBM_STORE_F64 ? 1 : (Codec<STORE
     typename Codec<STORE>::T* __restrict__ fout, const int32_t* __restrict__ map, const uint32_t* __restrict__ coord,
     const typename Codec<STORE>::R* __restrict__ ns, typename Codec<STORE>::R* __restrict__ face_stale,
     typename Codec<STORE>::R* __restrict__ vprev, typename Codec<STORE>::R* __restrict__ rho_out,
-    typename Codec<STORE>::R* __restrict__ v_out, const float* __restrict__ rref_in, float* __restrict__ rref_out) {
+    typename Codec<STORE>::R* __restrict__ v_out) {
     using Cd = Codec<STORE>;
     using R = typename Cd::R;
     // programmatic dependent launch, as in the single-phase step: the next
@@ -128,7 +137,7 @@ __global__ void __launch_bounds__(256, STORE == LBM_STORE_F64 ? 1 : (Codec<STORE
     asm volatile("griddepcontrol.wait;" ::: "memory");
 
     R F[19];
-    grey_gather_node<STORE>(F, fin, map, ns, n, C.nx, C.ny, C.nz, i, j, k, rref_in);
+    grey_gather_node<STORE>(F, fin, map, ns, n, C.nx, C.ny, C.nz, i, j, k, sp_ref(C));
 
     bool face = false;
     if (C.any_bc) {
@@ -175,7 +184,7 @@ __global__ void __launch_bounds__(256, STORE == LBM_STORE_F64 ? 1 : (Codec<STORE
     }
     // colission (GS:203-218): the single-phase MRT collision with the script's Guo term
     collide_sp<R, FORCE, Cd::DEV>(F, r, vx, vy, vz, C);
-    store_node<STORE>(F, fout, n, r, rref_out);
+    store_node<STORE>(F, fout, n, lbm_ref_at(sp_ref(C), i), C.seed);
 }
 
 template <int STORE, bool FORCE, bool MACROS>
@@ -196,7 +205,7 @@ int launch_grey(LbmHandle* h, const SpConsts<typename Codec<STORE>::R>& C, int g
     const cudaError_t e = cudaLaunchKernelEx(&cfg, grey_step_kernel<STORE, FORCE, MACROS>, C, fin, fout,
                                              (const int32_t*)h->d_map, (const uint32_t*)h->d_coord,
                                              (const R*)h->d_ns, (R*)h->d_gstale, (R*)h->d_vprev, (R*)h->d_rho,
-                                             (R*)h->d_v, (const float*)h->d_rref[h->cur], h->d_rref[h->cur ^ 1]);
+                                             (R*)h->d_v);
     h->cur ^= 1;
     return lbm_cuda_check(h, e != cudaSuccess ? e : cudaGetLastError(), "grey_step_kernel launch");
 }
@@ -204,10 +213,11 @@ int launch_grey(LbmHandle* h, const SpConsts<typename Codec<STORE>::R>& C, int g
 template <int STORE>
 int run_grey(LbmHandle* h, int32_t n, bool macros_last) {
     using R = typename Codec<STORE>::R;
-    const SpConsts<R> C = sp_make_consts<R>(h);
+    SpConsts<R> C = sp_make_consts<R>(h);
     const int grid = (int)((h->n_fluid + h->block - 1) / h->block);
     for (int32_t it = 0; it < n; ++it) {
         const bool mac = macros_last && it == n - 1;
+        C.seed = (uint32_t)(h->steps_done + it);
         int rc;
         if (h->force) rc = mac ? launch_grey<STORE, true, true>(h, C, grid) : launch_grey<STORE, true, false>(h, C, grid);
         else rc = mac ? launch_grey<STORE, false, true>(h, C, grid) : launch_grey<STORE, false, false>(h, C, grid);

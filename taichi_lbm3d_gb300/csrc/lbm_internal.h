@@ -40,6 +40,11 @@ struct SpConsts {
     // Deviation-form kernels: moments of the Guo term in closed form, M (w o g)
     // with g = gc (e - u).F + gd (e.u)(e.F); the (gc, gd) of the convention
     R gc, gd;
+    // 16-bit codecs: reference density of the stored deviations (x-linear
+    // between two fixed-pressure x faces, else 0) and the launch's step index
+    // (the stochastic-rounding seed)
+    R ref_a, ref_b;
+    uint32_t seed;
 };
 
 // int32 entries of -1 allocated after the dense map's last cell (bulk-copy rounding).
@@ -79,7 +84,6 @@ struct LbmHandle {
     void* d_vprev = nullptr;               // [3][np] previous-step v (pressure faces)
     void* d_rho = nullptr;                 // [np]
     void* d_v = nullptr;                   // [3][np]
-    float* d_rref[2] = {nullptr, nullptr}; // RHOREF storage: rho - 1 per node, ping-pong with f
     // two phase
     void* d_psi = nullptr;                 // [np] psi at fluid nodes
     void* d_rr[2] = {nullptr, nullptr};    // rho_r, double-buffered [np]

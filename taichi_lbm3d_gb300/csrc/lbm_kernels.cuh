@@ -55,6 +55,31 @@ static __device__ int g_lbm_debug_nlimit;
 __device__ __forceinline__ void lbm_debug_fail(int code) { atomicCAS(&g_lbm_debug, 0, code); }
 #endif
 
+template <typename R>
+__host__ __device__ __forceinline__ LbmRef<R> sp_ref(const SpConsts<R>& C) {
+    LbmRef<R> r;
+    r.a = C.ref_a;
+    r.b = C.ref_b;
+    return r;
+}
+
+// RHOREF codecs: the reference density at the node's x (ri) and the profile
+// (a + b x) for the sources: x - e_x, or the wrapped x on x-face warps.
+template <typename R>
+struct RefX {
+    R ri, a, b;
+};
+template <int STORE>
+__device__ __forceinline__ RefX<typename Codec<STORE>::R> ref_x(const LbmRef<typename Codec<STORE>::R>& ref, int i) {
+    RefX<typename Codec<STORE>::R> x{};
+    if constexpr (Codec<STORE>::RHOREF) {
+        x.a = ref.a;
+        x.b = ref.b;
+        x.ri = lbm_ref_at(ref, i);
+    }
+    return x;
+}
+
 template <int STORE, bool XWRAP>
 struct Gather {
     using Cd = Codec<STORE>;
@@ -63,7 +88,7 @@ struct Gather {
     template <int S>
     static __device__ __forceinline__ void one(R* F, const T* __restrict__ fin, const T* __restrict__ own,
                                                const int32_t* __restrict__ map, const Rows& rows, int i, int xm,
-                                               int xp, const float* __restrict__ rref, int n) {
+                                               int xp, const RefX<R>& rx) {
 #ifdef LBM_DEBUG
         int src = pull_source<S, XWRAP>(map, rows, i, xm, xp);
         if (g_lbm_debug_nlimit > 0 && src >= g_lbm_debug_nlimit) {
@@ -73,25 +98,32 @@ struct Gather {
 #else
         const int src = pull_source<S, XWRAP>(map, rows, i, xm, xp);
 #endif
-        load_pulled<S>(F, src, fin, own, rref, n);
+        load_pulled<S>(F, src, fin, own, rx, XWRAP ? (lbm_ex(S) > 0 ? xm : (lbm_ex(S) < 0 ? xp : i)) : i - lbm_ex(S));
     }
     // F[S] from the pull source node src (or the own LR[S] slot when src < 0):
     // one load from the selected address (+3% FP32, +4% FP32 deviation form on
-    // the 256^3 pack against two predicated loads).
+    // the 256^3 pack against two predicated loads).  RHOREF: plus w_S times the
+    // reference density at the source's x, xs (the node's own x for bounce-back).
     template <int S>
     static __device__ __forceinline__ void load_pulled(R* F, int src, const T* __restrict__ fin,
-                                                       const T* __restrict__ own, const float* __restrict__ rref,
-                                                       int n) {
+                                                       const T* __restrict__ own, const RefX<R>& rx, int xs) {
         const T* a = src >= 0 ? fin + lbm_eoff32(src) + 32 * S : own + 32 * lbm_lr(S);
         F[S] = Cd::template dec<S>(*a);
-        if constexpr (Cd::RHOREF) F[S] = lbm_fma<R>((R)lbm_w(S), (R)rref[src >= 0 ? src : n], F[S]);
+        if constexpr (Cd::RHOREF) {
+            R rs = rx.ri;
+            if constexpr (lbm_ex(S) != 0) {
+                if constexpr (XWRAP) rs = lbm_fma<R>(rx.b, (R)xs, rx.a);
+                else rs = lbm_ex(S) > 0 ? rx.ri - rx.b : rx.ri + rx.b;
+            }
+            F[S] = lbm_fma<R>((R)lbm_w(S), src >= 0 ? rs : rx.ri, F[S]);
+        }
     }
     static __device__ __forceinline__ void all(R* F, const T* __restrict__ fin, const T* __restrict__ own,
                                                const int32_t* __restrict__ map, const Rows& rows, int i, int xm,
-                                               int xp, const float* __restrict__ rref, int n) {
+                                               int xp, const RefX<R>& rx) {
         F[0] = Cd::template dec<0>(own[0]);
-        if constexpr (Cd::RHOREF) F[0] = lbm_fma<R>((R)lbm_w(0), (R)rref[n], F[0]);
-#define LBM_G(S) one<S>(F, fin, own, map, rows, i, xm, xp, rref, n);
+        if constexpr (Cd::RHOREF) F[0] = lbm_fma<R>((R)lbm_w(0), rx.ri, F[0]);
+#define LBM_G(S) one<S>(F, fin, own, map, rows, i, xm, xp, rx);
         LBM_G(1) LBM_G(2) LBM_G(3) LBM_G(4) LBM_G(5) LBM_G(6) LBM_G(7) LBM_G(8) LBM_G(9)
         LBM_G(10) LBM_G(11) LBM_G(12) LBM_G(13) LBM_G(14) LBM_G(15) LBM_G(16) LBM_G(17) LBM_G(18)
 #undef LBM_G
@@ -102,15 +134,17 @@ struct Gather {
 template <int STORE>
 __device__ __forceinline__ void gather_node(typename Codec<STORE>::R* F, const typename Codec<STORE>::T* __restrict__ fin,
                                             const int32_t* __restrict__ map, int n, int nx, int ny, int nz, int i, int j,
-                                            int k, const float* __restrict__ rref = nullptr) {
+                                            int k,
+                                            const LbmRef<typename Codec<STORE>::R>& ref = LbmRef<typename Codec<STORE>::R>()) {
     const int xm = i == 0 ? nx - 1 : i - 1, xp = i == nx - 1 ? 0 : i + 1;
     const int ym = j == 0 ? ny - 1 : j - 1, yp = j == ny - 1 ? 0 : j + 1;
     const int zm = k == 0 ? nz - 1 : k - 1, zp = k == nz - 1 ? 0 : k + 1;
     const Rows rows = make_rows(nx, ny, i, j, k, ym, yp, zm, zp);
     const typename Codec<STORE>::T* own = fin + lbm_eoff32(n);
+    const auto rx = ref_x<STORE>(ref, i);
     const bool x_inside = i > 0 && i < nx - 1;
-    if (__all_sync(__activemask(), x_inside)) Gather<STORE, false>::all(F, fin, own, map, rows, i, xm, xp, rref, n);
-    else Gather<STORE, true>::all(F, fin, own, map, rows, i, xm, xp, rref, n);
+    if (__all_sync(__activemask(), x_inside)) Gather<STORE, false>::all(F, fin, own, map, rows, i, xm, xp, rx);
+    else Gather<STORE, true>::all(F, fin, own, map, rows, i, xm, xp, rx);
 }
 
 // Gather through a shared-memory copy of the map: planes pz = 0, 1, 2 hold
@@ -126,7 +160,7 @@ struct GatherS {
     template <int S>
     static __device__ __forceinline__ void one(R* F, const T* __restrict__ fin, const T* __restrict__ own,
                                                const int32_t* sm, const int (&b)[3], int nx, int i, int xm, int xp,
-                                               const float* __restrict__ rref, int n) {
+                                               const RefX<R>& rx) {
         constexpr int ex = lbm_ex(S), ey = lbm_ey(S), ez = lbm_ez(S);
         int idx = b[1 - ez] - ey * nx;
         if constexpr (XWRAP) idx += (ex > 0 ? xm : (ex < 0 ? xp : i)) - i;
@@ -140,14 +174,14 @@ struct GatherS {
 #else
         const int src = sm[idx];
 #endif
-        G::template load_pulled<S>(F, src, fin, own, rref, n);
+        G::template load_pulled<S>(F, src, fin, own, rx, XWRAP ? (ex > 0 ? xm : (ex < 0 ? xp : i)) : i - ex);
     }
     static __device__ __forceinline__ void all(R* F, const T* __restrict__ fin, const T* __restrict__ own,
                                                const int32_t* sm, const int (&b)[3], int nx, int i, int xm, int xp,
-                                               const float* __restrict__ rref, int n) {
+                                               const RefX<R>& rx) {
         F[0] = Codec<STORE>::template dec<0>(own[0]);
-        if constexpr (Codec<STORE>::RHOREF) F[0] = lbm_fma<R>((R)lbm_w(0), (R)rref[n], F[0]);
-#define LBM_G(S) one<S>(F, fin, own, sm, b, nx, i, xm, xp, rref, n);
+        if constexpr (Codec<STORE>::RHOREF) F[0] = lbm_fma<R>((R)lbm_w(0), rx.ri, F[0]);
+#define LBM_G(S) one<S>(F, fin, own, sm, b, nx, i, xm, xp, rx);
         LBM_G(1) LBM_G(2) LBM_G(3) LBM_G(4) LBM_G(5) LBM_G(6) LBM_G(7) LBM_G(8) LBM_G(9)
         LBM_G(10) LBM_G(11) LBM_G(12) LBM_G(13) LBM_G(14) LBM_G(15) LBM_G(16) LBM_G(17) LBM_G(18)
 #undef LBM_G
@@ -158,30 +192,39 @@ template <int STORE>
 __device__ __forceinline__ void gather_node_smem(typename Codec<STORE>::R* F,
                                                  const typename Codec<STORE>::T* __restrict__ fin, const int32_t* sm,
                                                  const int (&b)[3], int n, int nx, int i,
-                                                 const float* __restrict__ rref = nullptr) {
+                                                 const LbmRef<typename Codec<STORE>::R>& ref) {
     const int xm = i == 0 ? nx - 1 : i - 1, xp = i == nx - 1 ? 0 : i + 1;
     const typename Codec<STORE>::T* own = fin + lbm_eoff32(n);
+    const auto rx = ref_x<STORE>(ref, i);
     const bool x_inside = i > 0 && i < nx - 1;
-    if (__all_sync(__activemask(), x_inside)) GatherS<STORE, false>::all(F, fin, own, sm, b, nx, i, xm, xp, rref, n);
-    else GatherS<STORE, true>::all(F, fin, own, sm, b, nx, i, xm, xp, rref, n);
+    if (__all_sync(__activemask(), x_inside)) GatherS<STORE, false>::all(F, fin, own, sm, b, nx, i, xm, xp, rx);
+    else GatherS<STORE, true>::all(F, fin, own, sm, b, nx, i, xm, xp, rx);
 }
 
 #define LBM_ALL_DIRS(X) X(1) X(2) X(3) X(4) X(5) X(6) X(7) X(8) X(9) X(10) X(11) X(12) X(13) X(14) X(15) X(16) X(17) X(18)
 
-// Store node n's post-collision populations; RHOREF codecs store them relative
-// to the node's density (g = f' - w r, r = rho - 1) and keep r.
+// Store node n's post-collision populations.  RHOREF codecs store them
+// relative to the reference density at the node's x (g = f' - w ref), rounded
+// stochastically with the bits of (n, seed) (LBM_SR).
 template <int STORE>
 __device__ __forceinline__ void store_node(const typename Codec<STORE>::R* F, typename Codec<STORE>::T* __restrict__ fout,
-                                           int n, typename Codec<STORE>::R r, float* __restrict__ rref_out) {
+                                           int n, typename Codec<STORE>::R ref_own, uint32_t seed) {
     using Cd = Codec<STORE>;
     using R = typename Cd::R;
     typename Cd::T* out = fout + lbm_eoff32(n);
     if constexpr (Cd::RHOREF) {
-#define LBM_S(S) out[32 * S] = Cd::template enc<S>(lbm_fma<R>(-(R)lbm_w(S), r, F[S]));
+#if LBM_SR
+        const uint32_t h = lbm_sr_hash((uint32_t)n, seed);
+#define LBM_S(S) out[32 * S] = Cd::template enc_sr<S>(lbm_fma<R>(-(R)lbm_w(S), ref_own, F[S]), h);
+#else
+        (void)seed;
+#define LBM_S(S) out[32 * S] = Cd::template enc<S>(lbm_fma<R>(-(R)lbm_w(S), ref_own, F[S]));
+#endif
         LBM_S(0) LBM_ALL_DIRS(LBM_S)
 #undef LBM_S
-        rref_out[n] = (float)r;
     } else {
+        (void)ref_own;
+        (void)seed;
 #define LBM_S(S) out[32 * S] = Cd::template enc<S>(F[S]);
         LBM_S(0) LBM_ALL_DIRS(LBM_S)
 #undef LBM_S

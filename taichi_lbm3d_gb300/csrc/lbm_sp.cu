@@ -47,6 +47,13 @@
 #ifndef LBM_SP_MINBLOCKS_DEV
 #define LBM_SP_MINBLOCKS_DEV 5
 #endif
+// The 16-bit codecs keep each direction's source reference (or the node's own,
+// for bounce-back) live across the population loads and spill at 48
+// registers: 4 CTAs per SM (64 registers) measured FP16 32.0k / BF16 32.5k
+// MLUPS against 29.5k / 30.2k at 5.
+#ifndef LBM_SP_MINBLOCKS_16
+#define LBM_SP_MINBLOCKS_16 4
+#endif
 // Programmatic dependent launch of consecutive steps: each step's CTAs may
 // become resident while the previous step drains and wait (griddepcontrol)
 // before touching populations or boundary state.  0 = plain stream order.
@@ -65,8 +72,7 @@ __device__ __forceinline__ void sp_finish_node(typename Codec<STORE>::R* F, int 
                                                const int32_t* __restrict__ map,
                                                typename Codec<STORE>::R* __restrict__ vprev,
                                                typename Codec<STORE>::R* __restrict__ rho_out,
-                                               typename Codec<STORE>::R* __restrict__ v_out,
-                                               float* __restrict__ rref_out) {
+                                               typename Codec<STORE>::R* __restrict__ v_out) {
     using Cd = Codec<STORE>;
     using R = typename Cd::R;
     const int64_t np = C.np;
@@ -104,12 +110,13 @@ __device__ __forceinline__ void sp_finish_node(typename Codec<STORE>::R* F, int 
     }
 
     collide_sp<R, FORCE, Cd::DEV>(F, r, vx, vy, vz, C);
-    store_node<STORE>(F, fout, n, r, rref_out);
+    store_node<STORE>(F, fout, n, lbm_ref_at(sp_ref(C), i), C.seed);
 }
 
 template <int STORE, bool FORCE, bool MACROS>
 __global__ void __launch_bounds__(256, STORE == LBM_STORE_F64 ? 1
-                                           : Codec<STORE>::DEV    ? LBM_SP_MINBLOCKS_DEV
+                                           : Codec<STORE>::RHOREF ? LBM_SP_MINBLOCKS_16
+                                       : Codec<STORE>::DEV    ? LBM_SP_MINBLOCKS_DEV
                                            : FORCE                ? 4
                                                                   : LBM_SP_MINBLOCKS)
     sp_step_kernel(const __grid_constant__ SpConsts<typename Codec<STORE>::R> C,
@@ -119,9 +126,7 @@ __global__ void __launch_bounds__(256, STORE == LBM_STORE_F64 ? 1
                                                       const uint32_t* __restrict__ coord,
                                                       typename Codec<STORE>::R* __restrict__ vprev,
                                                       typename Codec<STORE>::R* __restrict__ rho_out,
-                                                      typename Codec<STORE>::R* __restrict__ v_out,
-                                                      const float* __restrict__ rref_in,
-                                                      float* __restrict__ rref_out) {
+                                                      typename Codec<STORE>::R* __restrict__ v_out) {
     using Cd = Codec<STORE>;
     using R = typename Cd::R;
 #if LBM_SP_PDL
@@ -145,8 +150,8 @@ __global__ void __launch_bounds__(256, STORE == LBM_STORE_F64 ? 1
 #endif
 
     R F[19];
-    gather_node<STORE>(F, fin, map, n, C.nx, C.ny, C.nz, i, j, k, rref_in);
-    sp_finish_node<STORE, FORCE, MACROS>(F, n, i, j, k, C, fout, map, vprev, rho_out, v_out, rref_out);
+    gather_node<STORE>(F, fin, map, n, C.nx, C.ny, C.nz, i, j, k, sp_ref(C));
+    sp_finish_node<STORE, FORCE, MACROS>(F, n, i, j, k, C, fout, map, vprev, rho_out, v_out);
 }
 
 // ------------------------------------------------------------ staged step
@@ -282,6 +287,7 @@ __device__ __forceinline__ void spt_next(const SptArgs& A, int nx, int ny, int n
 
 template <int STORE, bool FORCE, bool MACROS>
 __global__ void __launch_bounds__(SPT, STORE == LBM_STORE_F64 ? 1
+                                       : Codec<STORE>::RHOREF ? LBM_SP_MINBLOCKS_16
                                        : Codec<STORE>::DEV    ? LBM_SP_MINBLOCKS_DEV
                                        : FORCE                ? 4
                                                               : LBM_SP_MINBLOCKS)
@@ -289,8 +295,7 @@ __global__ void __launch_bounds__(SPT, STORE == LBM_STORE_F64 ? 1
                    const typename Codec<STORE>::T* __restrict__ fin, typename Codec<STORE>::T* __restrict__ fout,
                    const int32_t* __restrict__ map, const uint32_t* __restrict__ coord,
                    typename Codec<STORE>::R* __restrict__ vprev, typename Codec<STORE>::R* __restrict__ rho_out,
-                   typename Codec<STORE>::R* __restrict__ v_out, const float* __restrict__ rref_in,
-                   float* __restrict__ rref_out) {
+                   typename Codec<STORE>::R* __restrict__ v_out) {
     using R = typename Codec<STORE>::R;
     extern __shared__ __align__(16) unsigned char spt_smem[];
     uint64_t* bars = reinterpret_cast<uint64_t*>(spt_smem);
@@ -353,9 +358,9 @@ __global__ void __launch_bounds__(SPT, STORE == LBM_STORE_F64 ? 1
                     spt_plane(pz, k, ti.x, C.nx, C.ny, C.nz, &first, &sh);
                     b[pz] = pz * A.plane + sh + (j - ti.x) * C.nx + i;
                 }
-                gather_node_smem<STORE>(F, fin, s_map, b, n, C.nx, i, rref_in);
+                gather_node_smem<STORE>(F, fin, s_map, b, n, C.nx, i, sp_ref(C));
             } else {
-                gather_node<STORE>(F, fin, map, n, C.nx, C.ny, C.nz, i, j, k, rref_in);
+                gather_node<STORE>(F, fin, map, n, C.nx, C.ny, C.nz, i, j, k, sp_ref(C));
             }
         }
         // this warp is done with the buffer; the last warp claims and stages the next tile
@@ -368,7 +373,7 @@ __global__ void __launch_bounds__(SPT, STORE == LBM_STORE_F64 ? 1
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             spt_next(A, C.nx, C.ny, C.nz, coord, map, bar, tiles + q, s_coord, s_map);
         }
-        if (active) sp_finish_node<STORE, FORCE, MACROS>(F, n, i, j, k, C, fout, map, vprev, rho_out, v_out, rref_out);
+        if (active) sp_finish_node<STORE, FORCE, MACROS>(F, n, i, j, k, C, fout, map, vprev, rho_out, v_out);
     }
 }
 
@@ -379,6 +384,7 @@ __global__ void __launch_bounds__(SPT, STORE == LBM_STORE_F64 ? 1
 // drain for the CTAs resident by then.
 template <int STORE, bool FORCE, bool MACROS>
 __global__ void __launch_bounds__(SPT, STORE == LBM_STORE_F64 ? 1
+                                       : Codec<STORE>::RHOREF ? LBM_SP_MINBLOCKS_16
                                        : Codec<STORE>::DEV    ? LBM_SP_MINBLOCKS_DEV
                                        : FORCE                ? 4
                                                               : LBM_SP_MINBLOCKS)
@@ -386,8 +392,7 @@ __global__ void __launch_bounds__(SPT, STORE == LBM_STORE_F64 ? 1
                     const typename Codec<STORE>::T* __restrict__ fin, typename Codec<STORE>::T* __restrict__ fout,
                     const int32_t* __restrict__ map, const uint32_t* __restrict__ coord,
                     typename Codec<STORE>::R* __restrict__ vprev, typename Codec<STORE>::R* __restrict__ rho_out,
-                    typename Codec<STORE>::R* __restrict__ v_out, const float* __restrict__ rref_in,
-                    float* __restrict__ rref_out) {
+                    typename Codec<STORE>::R* __restrict__ v_out) {
     using R = typename Codec<STORE>::R;
     extern __shared__ __align__(16) unsigned char spt_smem[];
     uint64_t* bar = reinterpret_cast<uint64_t*>(spt_smem);
@@ -450,9 +455,9 @@ __global__ void __launch_bounds__(SPT, STORE == LBM_STORE_F64 ? 1
     asm volatile("griddepcontrol.wait;" ::: "memory");
 #endif
     R F[19];
-    if (rows && !LBM_SPT_GLOBALMAP) gather_node_smem<STORE>(F, fin, s_map, b, n, C.nx, i, rref_in);
-    else gather_node<STORE>(F, fin, map, n, C.nx, C.ny, C.nz, i, j, k, rref_in);
-    sp_finish_node<STORE, FORCE, MACROS>(F, n, i, j, k, C, fout, map, vprev, rho_out, v_out, rref_out);
+    if (rows && !LBM_SPT_GLOBALMAP) gather_node_smem<STORE>(F, fin, s_map, b, n, C.nx, i, sp_ref(C));
+    else gather_node<STORE>(F, fin, map, n, C.nx, C.ny, C.nz, i, j, k, sp_ref(C));
+    sp_finish_node<STORE, FORCE, MACROS>(F, n, i, j, k, C, fout, map, vprev, rho_out, v_out);
 }
 
 size_t spt1_smem_bytes(int nx) { return SPT_HDR + SPT * 4 + 3 * (size_t)spt_plane_ints(nx) * 4; }
@@ -480,7 +485,7 @@ template <int STORE, bool FORCE>
 __global__ void sp_init_kernel(const __grid_constant__ SpConsts<typename Codec<STORE>::R> C,
                                typename Codec<STORE>::T* __restrict__ fout, const float* __restrict__ rho_in,
                                const float* __restrict__ v_in, typename Codec<STORE>::R* __restrict__ vprev,
-                               float* __restrict__ rref_out) {
+                               const uint32_t* __restrict__ coord) {
     using Cd = Codec<STORE>;
     using R = typename Cd::R;
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
@@ -501,7 +506,7 @@ __global__ void sp_init_kernel(const __grid_constant__ SpConsts<typename Codec<S
     vprev[2 * np + n] = vz;
     const R r = Cd::DEV ? rd : (R)1 + rd;
     collide_sp<R, FORCE, Cd::DEV>(F, r, vx, vy, vz, C);
-    store_node<STORE>(F, fout, n, r, rref_out);
+    store_node<STORE>(F, fout, n, lbm_ref_at(sp_ref(C), lbm_pi(coord[n])), ~C.seed);
 }
 
 // Pure pull-stream (identity collision, no faces): the permutation check.
@@ -536,8 +541,7 @@ int launch_step(LbmHandle* h, const SpConsts<typename Codec<STORE>::R>& C, int g
     cfg.numAttrs = LBM_SP_PDL ? 1 : 0;
     const cudaError_t e = cudaLaunchKernelEx(&cfg, sp_step_kernel<STORE, FORCE, MACROS>, C, fin, fout,
                                              (const int32_t*)h->d_map, (const uint32_t*)h->d_coord, (R*)h->d_vprev,
-                                             (R*)h->d_rho, (R*)h->d_v, (const float*)h->d_rref[h->cur],
-                                             h->d_rref[h->cur ^ 1]);
+                                             (R*)h->d_rho, (R*)h->d_v);
     h->cur ^= 1;
     return lbm_cuda_check(h, e != cudaSuccess ? e : cudaGetLastError(), "sp_step_kernel launch");
 }
@@ -565,16 +569,14 @@ int launch_tile(LbmHandle* h, const SpConsts<typename Codec<STORE>::R>& C, const
         cfg.dynamicSmemBytes = spt1_smem_bytes(h->p.nx);
         const cudaError_t e1 = cudaLaunchKernelEx(&cfg, sp_tile1_kernel<STORE, FORCE, MACROS>, C, a, fin, fout,
                                                   (const int32_t*)h->d_map, (const uint32_t*)h->d_coord,
-                                                  (R*)h->d_vprev, (R*)h->d_rho, (R*)h->d_v,
-                                                  (const float*)h->d_rref[h->cur], h->d_rref[h->cur ^ 1]);
+                                                  (R*)h->d_vprev, (R*)h->d_rho, (R*)h->d_v);
         const int rc1 = lbm_cuda_check(h, e1 != cudaSuccess ? e1 : cudaGetLastError(), "sp_tile1_kernel launch");
         if (!rc1) h->cur ^= 1;
         return rc1;
     }
     const cudaError_t e = cudaLaunchKernelEx(&cfg, sp_tile_kernel<STORE, FORCE, MACROS>, C, a, fin, fout,
                                              (const int32_t*)h->d_map, (const uint32_t*)h->d_coord, (R*)h->d_vprev,
-                                             (R*)h->d_rho, (R*)h->d_v, (const float*)h->d_rref[h->cur],
-                                             h->d_rref[h->cur ^ 1]);
+                                             (R*)h->d_rho, (R*)h->d_v);
     const int rc = lbm_cuda_check(h, e != cudaSuccess ? e : cudaGetLastError(), "sp_tile_kernel launch");
     if (!rc) {
         h->cur ^= 1;
@@ -597,7 +599,7 @@ int tile_grid(LbmHandle* h, size_t smem) {
 template <int STORE>
 int run_tiles(LbmHandle* h, int32_t n, bool macros_last) {
     using R = typename Codec<STORE>::R;
-    const SpConsts<R> C = sp_make_consts<R>(h);
+    SpConsts<R> C = sp_make_consts<R>(h);
     const size_t smem = spt_smem_bytes(h->p.nx);
     SptArgs A;
     A.tinfo = h->d_tinfo;
@@ -609,6 +611,7 @@ int run_tiles(LbmHandle* h, int32_t n, bool macros_last) {
     const int grid = h->force ? tile_grid<STORE, true>(h, smem) : tile_grid<STORE, false>(h, smem);
     for (int32_t it = 0; it < n; ++it) {
         const bool mac = macros_last && it == n - 1;
+        C.seed = (uint32_t)(h->steps_done + it);   // global step index: rounding bits of this step
         int rc;
         if (h->force) rc = mac ? launch_tile<STORE, true, true>(h, C, A, grid, smem) : launch_tile<STORE, true, false>(h, C, A, grid, smem);
         else rc = mac ? launch_tile<STORE, false, true>(h, C, A, grid, smem) : launch_tile<STORE, false, false>(h, C, A, grid, smem);
@@ -620,7 +623,7 @@ int run_tiles(LbmHandle* h, int32_t n, bool macros_last) {
 template <int STORE>
 int run_steps(LbmHandle* h, int32_t n, bool macros_last) {
     using R = typename Codec<STORE>::R;
-    const SpConsts<R> C = sp_make_consts<R>(h);
+    SpConsts<R> C = sp_make_consts<R>(h);
 #ifdef LBM_DEBUG
     int rc0 = lbm_cuda_check(h, cudaMemcpyToSymbolAsync(g_lbm_debug_nlimit, &h->n_fluid, sizeof(int), 0,
                                                         cudaMemcpyHostToDevice, h->stream),
@@ -632,6 +635,7 @@ int run_steps(LbmHandle* h, int32_t n, bool macros_last) {
     const int grid = (int)((h->n_fluid + h->block - 1) / h->block);
     for (int32_t it = 0; it < n; ++it) {
         const bool mac = macros_last && it == n - 1;
+        C.seed = (uint32_t)(h->steps_done + it);   // global step index: rounding bits of this step
         int rc;
         if (h->force) rc = mac ? launch_step<STORE, true, true>(h, C, grid) : launch_step<STORE, true, false>(h, C, grid);
         else rc = mac ? launch_step<STORE, false, true>(h, C, grid) : launch_step<STORE, false, false>(h, C, grid);
@@ -647,9 +651,9 @@ int run_init(LbmHandle* h, const float* rho, const float* v) {
     const SpConsts<R> C = sp_make_consts<R>(h);
     const int grid = (int)((h->n_fluid + h->block - 1) / h->block);
     T* fout = (T*)h->d_f[h->cur];
-    float* rref = h->d_rref[h->cur];
-    if (h->force) sp_init_kernel<STORE, true><<<grid, h->block, 0, h->stream>>>(C, fout, rho, v, (R*)h->d_vprev, rref);
-    else sp_init_kernel<STORE, false><<<grid, h->block, 0, h->stream>>>(C, fout, rho, v, (R*)h->d_vprev, rref);
+    const uint32_t* coord = h->d_coord;
+    if (h->force) sp_init_kernel<STORE, true><<<grid, h->block, 0, h->stream>>>(C, fout, rho, v, (R*)h->d_vprev, coord);
+    else sp_init_kernel<STORE, false><<<grid, h->block, 0, h->stream>>>(C, fout, rho, v, (R*)h->d_vprev, coord);
     return lbm_cuda_check(h, cudaGetLastError(), "sp_init_kernel launch");
 }
 
@@ -687,6 +691,15 @@ SpConsts<R> sp_make_consts(const LbmHandle* h) {
     // class (SP:236): /3, /9; scripts (TP:246): 1, 1; standard Guo: 3, 9
     C.gc = p.guo_convention == 0 ? (R)(1.0 / 3.0) : (p.guo_convention == 1 ? (R)1 : (R)3);
     C.gd = p.guo_convention == 0 ? (R)(1.0 / 9.0) : (p.guo_convention == 1 ? (R)1 : (R)9);
+    // reference density of the 16-bit codecs: the linear profile between the
+    // two x faces when both hold a fixed pressure, else 0
+    C.ref_a = (R)0;
+    C.ref_b = (R)0;
+    if (p.bc[0] == LBM_BC_PRESSURE && p.bc[1] == LBM_BC_PRESSURE && p.nx > 1) {
+        C.ref_a = (R)(p.rho_bc[0] - 1.0);
+        C.ref_b = (R)((p.rho_bc[1] - p.rho_bc[0]) / (double)(p.nx - 1));
+    }
+    C.seed = (uint32_t)h->steps_done;
     return C;
 }
 template SpConsts<float> sp_make_consts<float>(const LbmHandle*);

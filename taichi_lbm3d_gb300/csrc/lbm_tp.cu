@@ -198,8 +198,7 @@ __device__ __forceinline__ void tp_collide_and_store(typename Codec<STORE>::R* F
                                                      const typename Codec<STORE>::R* __restrict__ psi,
                                                      typename Codec<STORE>::R rr, typename Codec<STORE>::R rb,
                                                      typename Codec<STORE>::T* __restrict__ fout,
-                                                     typename Codec<STORE>::R* __restrict__ cs_out,
-                                                     float* __restrict__ rref_out) {
+                                                     typename Codec<STORE>::R* __restrict__ cs_out) {
     using Cd = Codec<STORE>;
     using R = typename Cd::R;
     R Cx, Cy, Cz;
@@ -214,7 +213,7 @@ __device__ __forceinline__ void tp_collide_and_store(typename Codec<STORE>::R* F
     R sv, so;
     s_local<R>(T, psi[n], sv, so);
     collide_tp<R, FORCE, Cd::DEV>(F, r, vx, vy, vz, cc, n0, n1, n2, sv, so, T);
-    store_node<STORE>(F, fout, n, r, rref_out);
+    store_node<STORE>(F, fout, n, lbm_ref_at(sp_ref(T.sp), i), T.sp.seed);
     R cs[9];
     recolour_amounts<R>(rr, rb, vx, vy, vz, Cx, Cy, Cz, cc, cs);
     const int64_t np = T.sp.np;
@@ -339,9 +338,7 @@ __global__ void __launch_bounds__(256) tp_flow_kernel(const __grid_constant__ Tp
                                                       const typename Codec<STORE>::R* __restrict__ rr,
                                                       const typename Codec<STORE>::R* __restrict__ rb,
                                                       const typename Codec<STORE>::R* __restrict__ psi,
-                                                      typename Codec<STORE>::R* __restrict__ cs_out,
-                                                      const float* __restrict__ rref_in,
-                                                      float* __restrict__ rref_out) {
+                                                      typename Codec<STORE>::R* __restrict__ cs_out) {
     using Cd = Codec<STORE>;
     using R = typename Cd::R;
     const SpConsts<R>& C = T.sp;
@@ -353,7 +350,7 @@ __global__ void __launch_bounds__(256) tp_flow_kernel(const __grid_constant__ Tp
     const int64_t np = C.np;
     tp_pdl_wait();  // rho_r, rho_b, psi of the colour launch; f, v, cs of the previous step
     R F[19];
-    gather_node<STORE>(F, fin, map, n, C.nx, C.ny, C.nz, i, j, k, rref_in);
+    gather_node<STORE>(F, fin, map, n, C.nx, C.ny, C.nz, i, j, k, sp_ref(C));
     if (C.any_bc && on_face(i, j, k, C, false)) apply_faces<R, Cd::DEV>(F, i, j, k, n, C, map, v);  // v: previous step
     R r = F[0];
 #pragma unroll
@@ -372,8 +369,7 @@ __global__ void __launch_bounds__(256) tp_flow_kernel(const __grid_constant__ Tp
     v[n] = vx;
     v[np + n] = vy;
     v[2 * np + n] = vz;
-    tp_collide_and_store<STORE, FORCE>(F, r, vx, vy, vz, n, i, j, k, T, map, psi, rr[n], rb[n], fout, cs_out,
-                                       rref_out);
+    tp_collide_and_store<STORE, FORCE>(F, r, vx, vy, vz, n, i, j, k, T, map, psi, rr[n], rb[n], fout, cs_out);
 }
 
 // Initial state (TP:174-187) and the first collision: rho = 1, v = 0, F = feq(1, 0),
@@ -384,7 +380,7 @@ __global__ void tp_init_kernel(const __grid_constant__ TpConsts<typename Codec<S
                                const uint32_t* __restrict__ coord, typename Codec<STORE>::R* __restrict__ v,
                                typename Codec<STORE>::R* __restrict__ rho_out, typename Codec<STORE>::R* __restrict__ rr,
                                typename Codec<STORE>::R* __restrict__ rb, const typename Codec<STORE>::R* __restrict__ psi,
-                               typename Codec<STORE>::R* __restrict__ cs_out, float* __restrict__ rref_out) {
+                               typename Codec<STORE>::R* __restrict__ cs_out) {
     using Cd = Codec<STORE>;
     using R = typename Cd::R;
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
@@ -403,7 +399,7 @@ __global__ void tp_init_kernel(const __grid_constant__ TpConsts<typename Codec<S
     if constexpr (Cd::DEV) lbm_feq_dev_all<R>((R)0, (R)0, (R)0, (R)0, F);
     else lbm_feq_all<R>((R)1.0, (R)0, (R)0, (R)0, F);
     tp_collide_and_store<STORE, FORCE>(F, Cd::DEV ? (R)0 : (R)1.0, (R)0, (R)0, (R)0, n, lbm_pi(pc), lbm_pj(pc),
-                                       lbm_pk(pc), T, map, psi, r0, b0, fout, cs_out, rref_out);
+                                       lbm_pk(pc), T, map, psi, r0, b0, fout, cs_out);
 }
 
 template <typename R>
@@ -449,8 +445,7 @@ int tp_init_t(LbmHandle* h) {
     const int grid = (int)((h->n_fluid + h->block - 1) / h->block);
     auto k = h->force ? tp_init_kernel<STORE, true> : tp_init_kernel<STORE, false>;
     k<<<grid, h->block, 0, h->stream>>>(T, (Tt*)h->d_f[0], h->d_map, h->d_coord, (R*)h->d_v, (R*)h->d_rho,
-                                        (R*)h->d_rr[0], (R*)h->d_rb[0], (const R*)h->d_psi, (R*)h->d_cs,
-                                        h->d_rref[0]);
+                                        (R*)h->d_rr[0], (R*)h->d_rb[0], (const R*)h->d_psi, (R*)h->d_cs);
     rc = lbm_cuda_check(h, cudaGetLastError(), "tp_init_kernel launch");
     if (!rc) rc = lbm_cuda_check(h, cudaStreamSynchronize(h->stream), "tp_init");
     return rc;
@@ -460,10 +455,11 @@ template <int STORE>
 int tp_steps_t(LbmHandle* h, int32_t nsteps) {
     using R = typename Codec<STORE>::R;
     using Tt = typename Codec<STORE>::T;
-    const TpConsts<R> T = make_tp<R>(h);
+    TpConsts<R> T = make_tp<R>(h);
     const int grid = (int)((h->n_fluid + h->block - 1) / h->block);
     auto kb = h->force ? tp_flow_kernel<STORE, true> : tp_flow_kernel<STORE, false>;
     for (int32_t it = 0; it < nsteps; ++it) {
+        T.sp.seed = (uint32_t)(h->steps_done + it);   // global step index: rounding bits of this step
         const int c = h->ccur;
         cudaError_t e = tp_launch_pdl(tp_colour_kernel<R>, grid, h->block, h->stream, T, (const R*)h->d_rr[c],
                                       (const R*)h->d_rb[c], (const R*)h->d_v, (const R*)h->d_cs, (R*)h->d_rr[c ^ 1],
@@ -474,8 +470,7 @@ int tp_steps_t(LbmHandle* h, int32_t nsteps) {
         h->ccur ^= 1;
         e = tp_launch_pdl(kb, grid, h->block, h->stream, T, (const Tt*)h->d_f[h->cur], (Tt*)h->d_f[h->cur ^ 1],
                           (const int32_t*)h->d_map, (const uint32_t*)h->d_coord, (R*)h->d_v, (R*)h->d_rho,
-                          (const R*)h->d_rr[h->ccur], (const R*)h->d_rb[h->ccur], (const R*)h->d_psi, (R*)h->d_cs,
-                          (const float*)h->d_rref[h->cur], h->d_rref[h->cur ^ 1]);
+                          (const R*)h->d_rr[h->ccur], (const R*)h->d_rb[h->ccur], (const R*)h->d_psi, (R*)h->d_cs);
         rc = lbm_cuda_check(h, e != cudaSuccess ? e : cudaGetLastError(), "tp_flow_kernel launch");
         if (rc) return rc;
         h->cur ^= 1;

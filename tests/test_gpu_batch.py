@@ -66,7 +66,9 @@ def test_batch_beyond_int32_population_offsets():
     """A batch whose populations span more than 2^31 elements: three
     384x384x300 all-fluid subvolumes (132,710,400 nodes, 2.52e9 elements) ahead
     of a porous one.  The last subvolume's state must match its own single
-    lattice bit for bit, and the uniform ones must stay uniform."""
+    lattice bit for bit, and the uniform ones must stay uniform up to the
+    FP16 encoder's stochastic rounding, which rounds each node with its own
+    random bits (spread of rho below 1e-5, of v_x below 1% of its mean)."""
     from taichi_lbm3d_gb300.batch import Batch
     big = np.zeros((384, 384, 300), np.int8)
     small = sphere_pack((32, 32, 32), 2.5, 5, 0.40, seed=52)
@@ -86,7 +88,9 @@ def test_batch_beyond_int32_population_offsets():
     rho_r, v_r = lat.macros()
     lat.close()
     assert np.array_equal(rho_s, rho_r) and np.array_equal(v_s, v_r)
-    assert np.all(rho_b == rho_b.flat[0]) and np.all(v_b[..., 0] == v_b.flat[0]) and v_b.flat[0] > 0
+    vx = v_b[..., 0].astype(np.float64)
+    assert np.ptp(rho_b) < 1e-5 and vx.mean() > 0 and np.ptp(vx) < 1e-2 * vx.mean()
+    assert np.abs(v_b[..., 1:]).max() < 1e-2 * vx.mean()
 
 
 def test_batch_with_an_all_solid_subvolume():

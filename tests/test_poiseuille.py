@@ -68,11 +68,12 @@ def test_oracle_channel_flow_matches_parabola(conv):
 # storage -> tolerance of the standard-convention profile on the GPU.  FP64
 # and the FP32 deviation form reproduce the parabola; FP32 reference
 # arithmetic carries the reference's own round-off (f ~ w, |u| ~ 3e-4: 0.9%,
-# the same as the FP32 oracle).  The 16-bit storages are regression bounds,
-# not accuracy claims: at steady state each step's forcing changes the stored
-# deviation by about 8 nu / H^2 ~ 3e-3 of itself, a few FP16 ulps and about
-# one BF16 ulp, so rounding stalls the profile (measured 3.8% and 31%).
-GPU_TOL = {"f64": 1e-8, "f32dev": 1e-3, "f32": 2e-2, "f16": 6e-2, "bf16": 0.4}
+# the same as the FP32 oracle).  At steady state each step's forcing changes a
+# stored 16-bit deviation by about 8 nu / H^2 ~ 3e-3 of itself, a few FP16 ulps
+# and about one BF16 ulp: rounded to nearest the profile stalls (3.8% and 31%
+# off); the encoders round stochastically, which keeps every stored value
+# unbiased, so the profile reaches the parabola up to rounding noise.
+GPU_TOL = {"f64": 1e-8, "f32dev": 1e-3, "f32": 2e-2, "f16": 1e-2, "bf16": 5e-2}
 
 
 @pytest.mark.gpu
