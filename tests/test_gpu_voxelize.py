@@ -70,3 +70,23 @@ def test_cli_writes_vtk_and_geometry(tmp_path):
     assert flags.shape == (120, 20, 60)
     from taichi_lbm3d_gb300.geometry import read_ascii_geometry
     assert np.array_equal(read_ascii_geometry(geo, (120, 20, 60)), flags.astype(np.int8))
+
+
+def test_gpu_flags_match_the_reference_tools_fast_winding_rule():
+    """The reference tool (Convert_stl_to_binary.cpp:117-123) marks a point solid
+    when its libigl fast-winding-number signed distance is <= 0: |w_fast| >= 1/2,
+    or the point on the surface.  With w_fast restated from the published
+    algorithm (oracle/fwn_oracle.py), the GPU flags equal that rule at every grid
+    point of the reference box for the closed NACA 0012 wing, apart from the FP32
+    distance band of the test above."""
+    from oracle import fwn_oracle as F
+    make, origin, dx, dims = CASES["naca0012_reference_box"]
+    tris = make()
+    g_solid = vx.voxelize(tris, origin, None, dx, dims=dims)
+    pts = F.grid_points(origin, dx, dims)
+    wf = F.fast_winding_number(F.build_tree(tris), pts.reshape(-1, 3)).reshape(dims)
+    dist = oracle.mesh_distance(tris, origin, dx, dims)
+    eps = 1e-5 * dx
+    ref_solid = ((np.abs(wf) >= 0.5) | (dist <= eps)).astype(np.int8)
+    band = np.abs(dist - eps) < 0.5 * eps
+    assert np.array_equal(g_solid[~band], ref_solid[~band]), int((g_solid != ref_solid)[~band].sum())

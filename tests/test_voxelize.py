@@ -72,3 +72,51 @@ def test_vtk_structured_points_roundtrip(tmp_path):
     assert txt[0] == "# vtk DataFile Version 2.0" and txt[3] == "DATASET STRUCTURED_POINTS"
     assert "DIMENSIONS 5 4 3" in txt and "POINT_DATA 60" in txt
     assert np.array_equal(vx.read_vtk_structured_points(path), f)
+
+
+def _fwn_vs_exact(tris, origin, dx, dims):
+    from oracle import fwn_oracle as F
+    tree = F.build_tree(tris)
+    pts = F.grid_points(origin, dx, dims).reshape(-1, 3)
+    wf = F.fast_winding_number(tree, pts).reshape(dims).ravel(order="F")
+    _, w = oracle.voxelize(tris, origin, dx, dims)
+    d = oracle.mesh_distance(tris, origin, dx, dims).reshape(-1, order="F")
+    return wf, w.reshape(-1, order="F"), d
+
+
+@pytest.mark.parametrize("mesh", ["sphere", "torus", "naca0012_reference_box"])
+def test_fast_winding_number_matches_exact_classification(mesh):
+    """The reference tool classifies with libigl's fast winding number (order-2
+    far field, accuracy 2); restated in oracle/fwn_oracle.py it stays within a
+    few 1e-3 of the exact winding number off the surface, and on these closed
+    meshes, where the exact number is 0 or 1 off the surface, both rules mark the
+    same grid points solid (points on a triangle are solid by the distance rule)."""
+    tris, origin, dx, dims = {
+        "sphere": (vx.icosphere((0.1, -0.2, 0.3), 7.0, subdiv=3), (-9.5, -9.5, -9.5), 1.0, (20, 20, 20)),
+        "torus": (vx.torus((0, 0, 0), 6.0, 2.0), (-9.25, -9.25, -4.25), 0.5, (38, 38, 18)),
+        "naca0012_reference_box": (vx.naca4_wing("0012"), vx.REF_LO, vx.REF_DX,
+                                   vx.grid_dims(vx.REF_LO, vx.REF_HI, vx.REF_DX)),
+    }[mesh]
+    wf, w, d = _fwn_vs_exact(tris, origin, dx, dims)
+    off = d > 1e-5 * dx
+    err = np.abs(wf - w)[off]
+    print("%s: max |w_fast - w| off the surface %.2e" % (mesh, err.max()))
+    assert err.max() < 1e-2
+    assert np.array_equal(np.abs(wf[off]) >= 0.5, np.abs(w[off]) >= 0.5)
+
+
+def test_fast_winding_number_band_on_an_open_mesh():
+    """A sphere with 4 triangles removed: the winding number is fractional near
+    the hole, and the fast and exact classifications may differ only where the
+    exact |w| lies within the fast method's error of 1/2 (the unpinned band)."""
+    tris = vx.icosphere((0.1, -0.2, 0.3), 7.0, subdiv=3)
+    top = np.argsort(tris[:, :, 2].mean(axis=1))[-4:]
+    tris = np.delete(tris, top, axis=0)
+    origin, dx, dims = (-9.5, -9.5, -9.5), 1.0, (20, 20, 20)
+    wf, w, d = _fwn_vs_exact(tris, origin, dx, dims)
+    off = d > 1e-5 * dx
+    err = np.abs(wf - w)[off].max()
+    differ = (np.abs(wf) >= 0.5) != (np.abs(w) >= 0.5)
+    band = np.abs(np.abs(w) - 0.5) <= err
+    assert ((w[off] > 0.02) & (w[off] < 0.98)).any()        # fractional winding numbers exist
+    assert not (differ & off & ~band).any()
