@@ -509,6 +509,65 @@ def unet_step(steps=10, warmup=3, n=2, edge=96, activation="relu"):
             "loss_finite": bool(torch.isfinite(loss).all().item())}
 
 
+# (cin, cout, level) of the warm-start network's convolutions; level l runs on edge >> l
+UNET_LAYER_SHAPES = [(16, 16, 0), (16, 32, 1), (32, 32, 1), (32, 64, 2), (64, 64, 2), (96, 32, 1), (48, 16, 0)]
+
+
+def unet_layers(n=2, edge=96, iters=20):
+    """Per-layer 3x3x3 convolution kernels of the warm-start network on n x edge^3:
+    forward (ReLU epilogue), backward-data (the transposed shape, masked
+    epilogue) and weight gradient, each timed alone with CUDA events over
+    `iters` launches after 3 warm-up launches; TFLOP/s = 2 x voxels x 27 x
+    cin x cout per launch."""
+    import ctypes
+    import torch
+    from taichi_lbm3d_gb300 import unet
+    L = unet._lib()
+    p = lambda t: ctypes.c_void_p(t.data_ptr()) if t is not None else None
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def timed(f):
+        for _ in range(3):
+            assert f() == 0
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(iters):
+            f()
+        e1.record()
+        e1.synchronize()
+        return e0.elapsed_time(e1) / iters * 1e3
+
+    rows = []
+    torch.manual_seed(0)
+    for cin, cout, lv in UNET_LAYER_SHAPES:
+        e = edge >> lv
+        fl = 2.0 * n * e ** 3 * 27 * cin * cout
+        x = torch.randn((n, e, e, e, cin), device="cuda").to(torch.bfloat16)
+        g = torch.randn((n, e, e, e, cout), device="cuda").to(torch.bfloat16)
+        w = (torch.randn((cout, 27, cin), device="cuda") / (27 * cin) ** 0.5).to(torch.bfloat16)
+        wt = (torch.randn((cin, 27, cout), device="cuda") / (27 * cout) ** 0.5).to(torch.bfloat16)
+        b = torch.randn(cout, device="cuda")
+        y = torch.empty((n, e, e, e, cout), device="cuda", dtype=torch.bfloat16)
+        gx = torch.empty((n, e, e, e, cin), device="cuda", dtype=torch.bfloat16)
+        dw = torch.zeros((cout, 27, cin), device="cuda")
+        db = torch.zeros(cout, device="cuda")
+        scr = torch.empty(int(L.lbm_nn_wgrad_scratch_floats(n, e, e, e, cin, cout)), device="cuda")
+        us_f = timed(lambda: L.lbm_nn_conv3d_act(p(x), p(w), p(b), None, p(y), None, n, e, e, e, cin, cout, 0, s))
+        us_d = timed(lambda: L.lbm_nn_conv3d_act(p(g), p(wt), None, p(x), p(gx), None, n, e, e, e, cout, cin, 1, s))
+        us_w = timed(lambda: L.lbm_nn_conv3d_wgrad(p(x), p(g), p(dw), p(db), p(scr), scr.numel(), n, e, e, e, cin,
+                                                   cout, s))
+        flag = ctypes.c_int32(0)
+        assert L.lbm_nn_tc_status(ctypes.byref(flag)) == 0 and flag.value == 0
+        rows.append({"cin": cin, "cout": cout, "edge": e,
+                     "fwd_us": us_f, "fwd_tflops": fl / us_f / 1e6,
+                     "bwd_data_us": us_d, "bwd_data_tflops": fl / us_d / 1e6,
+                     "wgrad_us": us_w, "wgrad_tflops": fl / us_w / 1e6})
+    return {"workload": "warm-start U-Net convolution layers, %d x %d^3 at level 0, random data" % (n, edge),
+            "paths": {k: os.environ.get(k, "default") for k in ("LBM_NN_HALO", "LBM_NN_TMA", "LBM_NN_HALO_TD")},
+            "layers": rows}
+
+
 def grey_field(shape=SHAPE):
     """Grey-scale workload: the 256^3 pack of the default bench with ns = 1 in
     the spheres and a grey layer ns = 0.25 on pore cells within 1.5 cells of a
@@ -637,6 +696,8 @@ def main():
     ap.add_argument("--grey", action="store_true", help="grey-scale (partial bounce-back) step on a 256^3 grey field")
     ap.add_argument("--voxelize", action="store_true", help="STL voxeliser on a NACA wing in the reference box")
     ap.add_argument("--unet", action="store_true", help="warm-start U-Net training step on 2 x 96^3")
+    ap.add_argument("--unet-layers", action="store_true",
+                    help="each U-Net convolution kernel (forward, backward-data, weight gradient) timed alone")
     ap.add_argument("--cavity", action="store_true", help="64^3 lid-driven cavity, GPU vs CPU oracle")
     a = ap.parse_args()
     if a.cavity:
@@ -644,6 +705,9 @@ def main():
         return 0
     if a.voxelize:
         print(json.dumps({"voxelize": voxelize_bench()}))
+        return 0
+    if a.unet_layers:
+        print(json.dumps({"unet_layers": unet_layers(iters=a.steps or 20)}))
         return 0
     if a.unet:
         print(json.dumps({"unet": unet_step(steps=a.steps or 10),

@@ -130,3 +130,16 @@ int tp_launch_steps(LbmHandle* h, int32_t n, bool macros_last);
 
 // reductions (lbm_reduce.cu)
 int red_launch(LbmHandle* h, LbmStats* out, float* max_v_f32);
+
+// TMA-fed 3x3x3 convolution (nn_tma.cu).
+bool nn_tma_usable(int cin, int cout);
+int nn_conv3d_tma(const void* in, const void* w, const float* bias, const void* mask, void* out, void* pre, int n, int d,
+                  int h, int wd, int cin, int cout, int mode, cudaStream_t s);
+int nn_tma_take_error(int* flag);
+bool nn_halo_usable(int cin, int cout);
+int nn_conv3d_halo(const void* in, const void* w, const float* bias, const void* mask, void* out, void* pre, int n, int d,
+                   int h, int wd, int cin, int cout, int mode, cudaStream_t s);
+bool nn_wgrad_tma_usable(int cin, int cout);
+int64_t nn_wgrad_tma_chunks(int n, int d, int h, int w);
+int nn_wgrad_tma(const void* in, const void* g, float* part, float* dbpart, int n, int d, int h, int wd, int cin,
+                 int cout, cudaStream_t s);

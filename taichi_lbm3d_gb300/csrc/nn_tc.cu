@@ -589,6 +589,8 @@ int lbm_nn_conv3d_act(const void* in, const void* w, const float* bias, const vo
         return lbm_set_err(nullptr, LBM_EINVAL, "lbm_nn_conv3d: cin must be a multiple of 16 in [16, 128]; mode 0..3");
     if (mode == 2 && !pre) return lbm_set_err(nullptr, LBM_EINVAL, "lbm_nn_conv3d_act: mode 2 needs pre");
     cudaStream_t s = (cudaStream_t)stream;
+    if (nn_halo_usable(cin, cout)) return nn_conv3d_halo(in, w, bias, mask, out, pre, n, d, h, wd, cin, cout, mode, s);
+    if (nn_tma_usable(cin, cout)) return nn_conv3d_tma(in, w, bias, mask, out, pre, n, d, h, wd, cin, cout, mode, s);
     const bf16* I = (const bf16*)in;
     const bf16* Wt = (const bf16*)w;
     const bf16* M = (const bf16*)mask;
@@ -634,7 +636,9 @@ int lbm_nn_tc_status(int32_t* timed_out) {
     if (cudaMemcpyFromSymbol(&v, g_tc_error, sizeof(int)) != cudaSuccess ||
         cudaMemcpyToSymbol(g_tc_error, &zero, sizeof(int)) != cudaSuccess)
         return lbm_set_err(nullptr, LBM_ECUDA, "lbm_nn_tc_status: symbol copy failed");
-    *timed_out = v;
+    int vt = 0;
+    if (nn_tma_take_error(&vt) != LBM_OK) return lbm_set_err(nullptr, LBM_ECUDA, "lbm_nn_tc_status: symbol copy failed");
+    *timed_out = v | vt;
     return LBM_OK;
 }
 

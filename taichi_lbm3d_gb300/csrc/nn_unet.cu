@@ -6,6 +6,7 @@
 // The 3x3x3 convolution (forward, backward data) and its weight gradient run
 // on the tcgen05 tensor cores (nn_tc.cu); the weight gradient leaves one FP32
 // partial per (voxel chunk, tap), summed here in a fixed order.
+#include <algorithm>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -280,7 +281,8 @@ int check(const char* what) {
 extern "C" {
 
 int64_t lbm_nn_wgrad_scratch_floats(int32_t n, int32_t d, int32_t h, int32_t w, int32_t cin, int32_t cout) {
-    return nn_wgrad_tc_chunks((int64_t)n * d * h * w) * (27 * (int64_t)cin * cout + cout);
+    const int64_t chunks = std::max(nn_wgrad_tc_chunks((int64_t)n * d * h * w), nn_wgrad_tma_chunks(n, d, h, w));
+    return chunks * (27 * (int64_t)cin * cout + cout);
 }
 
 int lbm_nn_conv3d_wgrad(const void* in, const void* g, float* dw, float* db, float* scratch, int64_t scratch_floats,
@@ -290,9 +292,11 @@ int lbm_nn_conv3d_wgrad(const void* in, const void* g, float* dw, float* db, flo
     if (scratch_floats < lbm_nn_wgrad_scratch_floats(n, d, h, w, cin, cout))
         return lbm_set_err(nullptr, LBM_EINVAL, "lbm_nn_conv3d_wgrad: scratch too small");
     cudaStream_t s = (cudaStream_t)stream;
-    const int nchunk = (int)nn_wgrad_tc_chunks(nvox);
+    const bool tma = nn_wgrad_tma_usable(cin, cout);
+    const int nchunk = (int)(tma ? nn_wgrad_tma_chunks(n, d, h, w) : nn_wgrad_tc_chunks(nvox));
     float* dbpart = scratch + (int64_t)nchunk * 27 * cin * cout;
-    int rc = nn_wgrad_tc_launch(in, g, scratch, dbpart, n, d, h, w, cin, cout, s);
+    int rc = tma ? nn_wgrad_tma(in, g, scratch, dbpart, n, d, h, w, cin, cout, s)
+                 : nn_wgrad_tc_launch(in, g, scratch, dbpart, n, d, h, w, cin, cout, s);
     if (rc) return rc;
     wgrad_reduce_kernel<<<blocks((int64_t)27 * cin * cout), 256, 0, s>>>(scratch, dw, nchunk, cin, cout);
     rc = check("wgrad_reduce_kernel");
