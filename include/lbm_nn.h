@@ -19,7 +19,10 @@ extern "C" {
 #endif
 
 /* 3x3x3 convolution, zero padding, implicit GEMM on the tcgen05 tensor cores
- * (accumulator in tensor memory, 128 voxels per CTA).  mode 0:
+ * (accumulator in tensor memory, 128 voxels per accumulator).  Narrow layers
+ * read a shared-memory halo, the others TMA im2col loads; LBM_NN_HALO=0 and
+ * LBM_NN_TMA=0 in the environment (read once per process) select the next
+ * kernel down, the last one staging operands with the CTA's threads.  mode 0:
  * out = relu(conv(in, w) + bias); mode 1: out = conv(in, w) * (mask > 0)
  * (mask NULL: no mask) -- the backward-data pass with flip-transposed weights.
  * Any voxel count; cin a multiple of 16 up to 128; cout in {16, 32, 48, 64, 96}. */
@@ -43,7 +46,8 @@ int lbm_nn_tc_timeout_selftest(void* stream);
 int lbm_nn_flip_transpose(const void* w, void* wt, int32_t cin, int32_t cout, void* stream);
 /* Weight gradient dw[co][tap][ci] (FP32) and bias gradient db[co] (may be NULL)
  * of the conv with input `in` and output gradient `g`, on the tcgen05 tensor
- * cores (per-chunk FP32 partials summed in a fixed order); cin a multiple of
+ * cores with both operands read MN-major from TMA boxes (LBM_NN_TMA=0: staged
+ * by the CTA's threads); per-chunk FP32 partials summed in a fixed order; cin a multiple of
  * 16 up to 128, cout a multiple of 8 up to 64; scratch of
  * lbm_nn_wgrad_scratch_floats() floats. */
 int64_t lbm_nn_wgrad_scratch_floats(int32_t n, int32_t d, int32_t h, int32_t w, int32_t cin, int32_t cout);
