@@ -141,5 +141,9 @@ int nn_conv3d_halo(const void* in, const void* w, const float* bias, const void*
                    int h, int wd, int cin, int cout, int mode, cudaStream_t s);
 bool nn_wgrad_tma_usable(int cin, int cout);
 int64_t nn_wgrad_tma_chunks(int n, int d, int h, int w);
+bool nn_wgrad_ws_usable(int cin, int cout);
+int64_t nn_wgrad_ws_chunks(int n, int d, int h, int w);
+int nn_wgrad_ws(const void* in, const void* g, float* part, float* dbpart, int n, int d, int h, int wd, int cin, int cout,
+                cudaStream_t s);
 int nn_wgrad_tma(const void* in, const void* g, float* part, float* dbpart, int n, int d, int h, int wd, int cin,
                  int cout, cudaStream_t s);

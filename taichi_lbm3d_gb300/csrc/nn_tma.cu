@@ -318,6 +318,12 @@ __device__ __forceinline__ uint64_t mn_desc(uint32_t addr, uint32_t lbo, uint32_
     return d;
 }
 
+// Byte offset of 16-byte chunk c of row r in a swizzled K-row-major tile whose rows are `span`
+// bytes (1024-aligned base): the chunk index is XORed with the row bits of the swizzle pattern.
+__device__ __forceinline__ uint32_t swz(uint32_t r, uint32_t c, uint32_t span) {
+    return r * span + ((c ^ ((r * span >> 7) & (span / 16u - 1u))) << 4);
+}
+
 template <int COUT>
 __global__ void __launch_bounds__(TMA_THREADS) conv3d_wgrad_tma_kernel(const __grid_constant__ TmaWgradArgs P,
                                                                       float* __restrict__ part,
@@ -642,6 +648,231 @@ __global__ void __launch_bounds__(TMA_THREADS) conv3d_halo_kernel(const HaloArgs
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(P.ncol) : "memory");
 }
 
+// ---------------------------------------------------------------------------
+// Warp-specialised weight gradient for layers whose input and output are one
+// channel part each (16, 32 or 64 channels): the same GEMM, tap groups, ones
+// slot and partials as conv3d_wgrad_tma_kernel, but each 8 x 4 x 4 block is
+// loaded once -- one dense TMA box of the 10 x 6 x 6 input halo and one of g
+// (no swizzle) -- and a CTA runs all tap groups of its blocks, one TMEM
+// accumulator per group.
+//   warp 4, lane 0: TMA producer (two boxes per block, two buffers) and MMA
+//     issuer (8 K = 16 steps per block and group, two operand buffers);
+//   warps 0-3: build the operand buffer of each (block, group) step from the
+//     halo -- tap slot j row r is the halo voxel r shifted by the tap, written
+//     in the swizzled MN-major layout -- plus the g operand, then the epilogue.
+// mbarriers between the roles: tfull (TMA -> copy), tempty (copy -> producer,
+// 128 arrivals), ofull (copy -> MMA, 128 arrivals), oempty (MMA commit ->
+// copy), done.  Every wait is bounded; a timeout records the error flag and
+// the roles leave their loops, the producer first waiting (bounded) for the
+// loads it issued.
+constexpr int WS_THREADS = 160;
+
+struct WsArgs {
+    CUtensorMap halo;               // input, tiled 5-D (cin, W, H, D, N), box (cin, 10, 6, 6, 1), no swizzle
+    CUtensorMap gmap;               // g, tiled 5-D (cout, W, H, D, N), box (cout, 8, 4, 4, 1), no swizzle
+    int cin, cout, tg, ngroups;     // tap slots per group (128 / cin), groups (ceil(27 / tg))
+    uint32_t hbytes;                // bytes of the halo box
+    uint32_t tbytes;                // bytes of one TMA buffer (halo then g), 1024-aligned
+    uint32_t obytes;                // bytes of one operand buffer (32 KB of tap slots + g), 1024-aligned
+    uint32_t ncol;                  // TMEM columns (power of two >= ngroups x cout)
+    int shift[27];                  // byte offset of tap t's shift inside the halo
+    int nbw, nbh, nbd;
+    int64_t nblocks;
+    int chunk_blocks;               // blocks per CTA (and per partial)
+};
+
+template <int COUT>
+__global__ void __launch_bounds__(WS_THREADS, 1) conv3d_wgrad_ws_kernel(const __grid_constant__ WsArgs P,
+                                                                    float* __restrict__ part,
+                                                                    float* __restrict__ dbpart) {
+    extern __shared__ unsigned char dsmem[];
+    __shared__ __align__(8) uint64_t s_tfull[2], s_tempty[2], s_ofull[2], s_oempty[2], s_done;
+    __shared__ uint32_t s_taddr;
+    __shared__ int s_fail;
+
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const uint32_t base = (su32(dsmem) + 1023u) & ~1023u;
+    const uint32_t obase = base + 2u * P.tbytes;
+    const int64_t chunk = blockIdx.x;
+    const int64_t b0 = chunk * P.chunk_blocks;
+    const int nb = (int)min((int64_t)P.chunk_blocks, P.nblocks - b0);
+    const int pw = P.cin, tg = P.tg, ng = P.ngroups;
+    const uint32_t span = 2u * (uint32_t)pw;
+    const uint32_t gs = 2u * (uint32_t)COUT;
+    const int ntap_last = 27 - (ng - 1) * tg;            // taps of the last group; its slot ntap_last holds ones
+
+    if (tid == 0) {
+        for (int b = 0; b < 2; ++b) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&s_tfull[b])) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 128;" ::"r"(su32(&s_tempty[b])) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 128;" ::"r"(su32(&s_ofull[b])) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&s_oempty[b])) : "memory");
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&s_done)) : "memory");
+        s_fail = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(&s_taddr)),
+                     "r"(P.ncol)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t taddr = s_taddr;
+    const int nsteps = nb * ng;
+
+    if (warp == 4) {
+        if ((tid & 31) == 0) {   // producer + MMA issuer
+            const uint32_t tx = P.hbytes + 128u * gs;
+            auto issue = [&](int b) {
+                int64_t q = b0 + b;
+                const int bw = (int)(q % P.nbw);
+                q /= P.nbw;
+                const int bh = (int)(q % P.nbh);
+                q /= P.nbh;
+                const int bd = (int)(q % P.nbd);
+                const int n = (int)(q / P.nbd);
+                const int w0 = bw * WGB_W, h0 = bh * WGB_H, d0 = bd * WGB_D;
+                const uint32_t tb = base + (uint32_t)(b & 1) * P.tbytes;
+                const uint32_t bar = su32(&s_tfull[b & 1]);
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(tx) : "memory");
+                asm volatile(
+                    "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                    " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(tb),
+                    "l"(&P.halo), "r"(0), "r"(w0 - 1), "r"(h0 - 1), "r"(d0 - 1), "r"(n), "r"(bar)
+                    : "memory");
+                asm volatile(
+                    "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                    " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(tb + P.hbytes),
+                    "l"(&P.gmap), "r"(0), "r"(w0), "r"(h0), "r"(d0), "r"(n), "r"(bar)
+                    : "memory");
+            };
+            int issued = 0, landed = 0;
+            bool fail = false;
+            for (; issued < 2 && issued < nb; ++issued) issue(issued);
+            for (int st = 0; st < nsteps && !fail; ++st) {
+                const int b = st / ng, gi = st - b * ng, ob = st & 1;
+                if (!tma_wait(&s_ofull[ob], (uint32_t)((st >> 1) & 1))) { fail = true; break; }
+                if (gi == 0) landed = b + 1;   // the copy warps saw block b's loads complete
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t sa = obase + (uint32_t)ob * P.obytes;
+                const uint32_t acc = taddr + (uint32_t)(gi * COUT);
+#pragma unroll 1
+                for (int kk = 0; kk < 8; ++kk) {
+                    const uint64_t ad = mn_desc(sa + (uint32_t)kk * 16u * span, 128u * span, 8u * span, (int)span);
+                    const uint64_t bdsc =
+                        mn_desc(sa + 32768u + (uint32_t)kk * 16u * gs, 8u * gs, 8u * gs, (int)gs);
+                    mma_f16(acc, ad, bdsc, idesc_mn(128, COUT), (b | kk) != 0 ? 1u : 0u);
+                }
+                mma_commit(&s_oempty[ob]);
+                if (gi == ng - 1 && b + 2 < nb) {   // block b's halo is no longer read: load block b + 2 there
+                    if (!tma_wait(&s_tempty[b & 1], (uint32_t)((b >> 1) & 1))) { fail = true; break; }
+                    issue(b + 2);
+                    ++issued;
+                }
+            }
+            if (fail) {
+                for (int b = landed; b < issued; ++b) tma_wait(&s_tfull[b & 1], (uint32_t)((b >> 1) & 1));
+                s_fail = 1;
+                atomicExch(&g_tma_error, 1);
+            }
+            mma_commit(&s_done);
+        }
+    } else {
+        // copy warps: the per-thread chunks of a step are fixed; tap t adds P.shift[t] to the source
+        const int csh = pw == 64 ? 3 : (pw == 32 ? 2 : 1);
+        // packed: source offset in the halo (< 46 KB) | destination offset in the tap slots (< 32 KB) << 16
+        uint32_t pk[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            const int e = tid + k * 128;
+            const int c = e & ((1 << csh) - 1);
+            const int r = (e >> csh) & 127;
+            const int j = e >> (7 + csh);                     // tap slot (< tg)
+            const int x = r & 7, y = (r >> 3) & 3, z = r >> 5;   // voxel of the block; halo origin at -1
+            const uint32_t src = (uint32_t)((z * 6 + y) * 10 + x) * span + (uint32_t)c * 16u;
+            const uint32_t dst = (uint32_t)j * 128u * span + swz((uint32_t)r, (uint32_t)c, span);
+            pk[k] = src | (dst << 16);
+        }
+        const int gch = COUT / 8;                             // g chunks per row
+        bool fail = false;
+        for (int st = 0; st < nsteps; ++st) {
+            const int b = st / ng, gi = st - b * ng, ob = st & 1;
+            if (gi == 0 && !tma_wait(&s_tfull[b & 1], (uint32_t)((b >> 1) & 1))) { fail = true; break; }
+            if (st >= 2 && !tma_wait(&s_oempty[ob], (uint32_t)(((st - 2) >> 1) & 1))) { fail = true; break; }
+            const uint32_t tsh = base + (uint32_t)(b & 1) * P.tbytes;
+            const uint32_t osh = obase + (uint32_t)ob * P.obytes;
+            const int ntap = gi == ng - 1 ? ntap_last : tg;
+#pragma unroll
+            for (int k = 0; k < 16; ++k) {
+                const int j = (tid + k * 128) >> (7 + csh);
+                if (j < ntap) {
+                    uint32_t v0, v1, v2, v3;
+                    asm volatile("ld.shared.v4.u32 {%0, %1, %2, %3}, [%4];"
+                                 : "=r"(v0), "=r"(v1), "=r"(v2), "=r"(v3)
+                                 : "r"(tsh + (pk[k] & 0xFFFFu) + (uint32_t)P.shift[gi * tg + j]));
+                    asm volatile("st.shared.v4.u32 [%0], {%1, %2, %3, %4};" ::"r"(osh + (pk[k] >> 16)), "r"(v0), "r"(v1),
+                                 "r"(v2), "r"(v3)
+                                 : "memory");
+                } else if (gi == ng - 1 && j == ntap) {          // the ones slot of the last group
+                    const uint32_t one = 0x3F803F80u;
+                    asm volatile("st.shared.v4.u32 [%0], {%1, %1, %1, %1};" ::"r"(osh + (pk[k] >> 16)), "r"(one) : "memory");
+                }
+            }
+            for (int e = tid; e < 128 * gch; e += 128) {        // g operand: row r, chunk c8
+                const int c8 = e % gch, r = e / gch;
+                uint32_t v0, v1, v2, v3;
+                asm volatile("ld.shared.v4.u32 {%0, %1, %2, %3}, [%4];"
+                             : "=r"(v0), "=r"(v1), "=r"(v2), "=r"(v3)
+                             : "r"(tsh + P.hbytes + (uint32_t)r * gs + (uint32_t)c8 * 16u));
+                asm volatile("st.shared.v4.u32 [%0], {%1, %2, %3, %4};" ::"r"(osh + 32768u + swz((uint32_t)r, (uint32_t)c8, gs)),
+                             "r"(v0), "r"(v1), "r"(v2), "r"(v3)
+                             : "memory");
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(&s_ofull[ob])) : "memory");
+            if (gi == ng - 1)   // done reading block b's halo and g
+                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(&s_tempty[b & 1])) : "memory");
+        }
+        if (fail) {
+            s_fail = 1;
+            if (tid == 0) atomicExch(&g_tma_error, 1);
+        }
+        if (!tma_wait(&s_done, 0)) s_fail = 1;
+    }
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (s_fail) {
+        if (tid == 0) atomicExch(&g_tma_error, 1);
+    } else if (warp < 4) {
+        const int sl = tid / pw, cil = tid % pw;
+        const uint32_t tw = taddr + ((uint32_t)(warp * 32) << 16);
+        for (int gi = 0; gi < ng; ++gi) {
+            const int ntap = gi == ng - 1 ? ntap_last : tg;
+#pragma unroll
+            for (int c0 = 0; c0 < COUT; c0 += 16) {
+                float acc[16];
+                tmem_ld16(tw + (uint32_t)(gi * COUT + c0), acc);
+                if (sl < ntap) {
+                    float* dst = part + ((chunk * 27 + gi * tg + sl) * COUT + c0) * P.cin + cil;
+#pragma unroll
+                    for (int q = 0; q < 16; ++q) dst[(int64_t)q * P.cin] = acc[q];
+                } else if (gi == ng - 1 && sl == ntap && cil == 0) {
+#pragma unroll
+                    for (int q = 0; q < 16; ++q) dbpart[chunk * COUT + c0 + q] = acc[q];
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(P.ncol) : "memory");
+}
+
 // Driver entry points for the tensor maps, resolved through the runtime.
 typedef CUresult(CUDAAPI* EncIm2col)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                      const cuuint64_t*, const int*, const int*, cuuint32_t, cuuint32_t,
@@ -950,6 +1181,108 @@ int nn_wgrad_tma(const void* in, const void* g, float* part, float* dbpart, int 
 #undef LBM_WGT
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return lbm_set_err(nullptr, LBM_ECUDA, std::string("conv3d_wgrad_tma_kernel: ") + cudaGetErrorString(e));
+    return LBM_OK;
+}
+
+// Warp-specialised weight gradient: one-part layers (cin and cout in {16, 32, 64})
+// whose accumulators (groups x cout columns) and buffers fit.  It is taken where
+// two CTAs fit an SM (113 KB) or cout = 64 > cin: with one CTA per SM the
+// TMA-box kernel was faster on 16 -> 32 and 32 -> 32 (2 x 48^3), while on 32 -> 64
+// the per-group reload of the 64-channel g made that kernel the slower one.
+// LBM_NN_WS=0 in the environment turns it off.
+static bool ws_plan(int cin, int cout, WsArgs* P, size_t* smem) {
+    if (!(cin == 16 || cin == 32 || cin == 64) || !(cout == 16 || cout == 32 || cout == 64)) return false;
+    P->cin = cin;
+    P->cout = cout;
+    P->tg = 128 / cin;
+    P->ngroups = (27 + P->tg - 1) / P->tg;
+    if (P->ngroups * cout > 512) return false;
+    P->ncol = 32;
+    while (P->ncol < (uint32_t)(P->ngroups * cout)) P->ncol <<= 1;
+    P->hbytes = 360u * (uint32_t)cin * 2u;
+    P->tbytes = (P->hbytes + 128u * 2u * (uint32_t)cout + 1023u) & ~1023u;
+    P->obytes = 32768u + ((128u * 2u * (uint32_t)cout + 1023u) & ~1023u);
+    for (int t = 0; t < 27; ++t) P->shift[t] = ((t / 9) * 60 + ((t / 3) % 3) * 10 + t % 3) * cin * 2;
+    *smem = 2 * (size_t)P->tbytes + 2 * (size_t)P->obytes + 1024;
+    return *smem <= 227 * 1024;
+}
+
+// Blocks per CTA: enough CTAs for about eight per SM of a 152-SM GPU, 2 to 32 blocks each.
+static int ws_chunk_blocks(int64_t nblocks) {
+    const int64_t c = (nblocks + 1215) / 1216;
+    return (int)std::min<int64_t>(WGB_CHUNK, std::max<int64_t>(2, c));
+}
+
+int64_t nn_wgrad_ws_chunks(int n, int d, int h, int w) {
+    const int64_t nb = wgrad_tma_blocks(n, d, h, w);
+    const int cb = ws_chunk_blocks(nb);
+    return (nb + cb - 1) / cb;
+}
+
+bool nn_wgrad_ws_usable(int cin, int cout) {
+    static const bool on = [] {
+        const char* e = getenv("LBM_NN_WS");
+        return !(e && e[0] == '0');
+    }();
+    WsArgs P{};
+    size_t smem = 0;
+    if (!on || !encoders() || !ws_plan(cin, cout, &P, &smem)) return false;
+    return smem <= 113 * 1024 || (cout == 64 && cin < cout);
+}
+
+// Partials for nn_wgrad_ws_chunks(n, d, h, w) chunks of the same 8 x 4 x 4 blocks.
+int nn_wgrad_ws(const void* in, const void* g, float* part, float* dbpart, int n, int d, int h, int wd, int cin, int cout,
+                cudaStream_t s) {
+    if (!encoders()) return lbm_set_err(nullptr, LBM_ECUDA, "lbm_nn_conv3d_wgrad (ws): tensor-map entry points unavailable");
+    WsArgs P{};
+    size_t smem = 0;
+    if (!ws_plan(cin, cout, &P, &smem)) return lbm_set_err(nullptr, LBM_EINVAL, "lbm_nn_conv3d_wgrad (ws): unsupported channels");
+    P.nbw = (wd + WGB_W - 1) / WGB_W;
+    P.nbh = (h + WGB_H - 1) / WGB_H;
+    P.nbd = (d + WGB_D - 1) / WGB_D;
+    P.nblocks = wgrad_tma_blocks(n, d, h, wd);
+    P.chunk_blocks = ws_chunk_blocks(P.nblocks);
+    const cuuint32_t es[5] = {1, 1, 1, 1, 1};
+    {
+        const cuuint64_t dim[5] = {(cuuint64_t)cin, (cuuint64_t)wd, (cuuint64_t)h, (cuuint64_t)d, (cuuint64_t)n};
+        const cuuint64_t str[4] = {(cuuint64_t)cin * 2, (cuuint64_t)wd * cin * 2, (cuuint64_t)h * wd * cin * 2,
+                                   (cuuint64_t)d * h * wd * cin * 2};
+        const cuuint32_t box[5] = {(cuuint32_t)cin, 10, 6, 6, 1};
+        const CUresult r = g_enc_tiled(&P.halo, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void*>(in), dim, str, box,
+                                       es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                       CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS)
+            return lbm_set_err(nullptr, LBM_ECUDA, "lbm_nn_conv3d_wgrad (ws): halo tensor map, error " + std::to_string((int)r));
+    }
+    {
+        const cuuint64_t dim[5] = {(cuuint64_t)cout, (cuuint64_t)wd, (cuuint64_t)h, (cuuint64_t)d, (cuuint64_t)n};
+        const cuuint64_t str[4] = {(cuuint64_t)cout * 2, (cuuint64_t)wd * cout * 2, (cuuint64_t)h * wd * cout * 2,
+                                   (cuuint64_t)d * h * wd * cout * 2};
+        const cuuint32_t box[5] = {(cuuint32_t)cout, WGB_W, WGB_H, WGB_D, 1};
+        const CUresult r = g_enc_tiled(&P.gmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void*>(g), dim, str, box,
+                                       es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                       CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS)
+            return lbm_set_err(nullptr, LBM_ECUDA, "lbm_nn_conv3d_wgrad (ws): g tensor map, error " + std::to_string((int)r));
+    }
+    const int64_t nchunk = nn_wgrad_ws_chunks(n, d, h, wd);
+    if (nchunk > 2147483647LL) return lbm_set_err(nullptr, LBM_EINVAL, "lbm_nn_conv3d_wgrad (ws): too many chunks");
+#define LBM_WS(C)                                                                                                \
+    case C: {                                                                                                    \
+        auto k = conv3d_wgrad_ws_kernel<C>;                                                                      \
+        if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)      \
+            return lbm_set_err(nullptr, LBM_ECUDA, "lbm_nn_conv3d_wgrad (ws): shared memory attribute refused"); \
+        k<<<(unsigned)nchunk, WS_THREADS, smem, s>>>(P, part, dbpart);                                           \
+        break;                                                                                                   \
+    }
+    switch (cout) {
+        LBM_WS(16) LBM_WS(32) LBM_WS(64)
+    default:
+        return lbm_set_err(nullptr, LBM_EINVAL, "lbm_nn_conv3d_wgrad (ws): unsupported cout");
+    }
+#undef LBM_WS
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return lbm_set_err(nullptr, LBM_ECUDA, std::string("conv3d_wgrad_ws_kernel: ") + cudaGetErrorString(e));
     return LBM_OK;
 }
 

@@ -42,25 +42,50 @@ __device__ __forceinline__ Vox decode(int64_t v, int D, int H, int W) {
 }
 
 // dw[co][tap][ci] = sum over chunks (fixed order) of part[chunk][tap][co][ci].
-__global__ void wgrad_reduce_kernel(const float* __restrict__ part, float* __restrict__ dw, int nchunk, int cin,
-                                    int cout) {
-    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(256) wgrad_reduce_kernel(const float* __restrict__ part, float* __restrict__ dw,
+                                                            int nchunk, int cin, int cout) {
+    // 32 consecutive elements per CTA (one 128-byte row per chunk); warp w sums chunks w, w + 8, ...
+    // in that order, then the 8 warp sums are added in warp order: a fixed order for any launch
+    __shared__ float s_part[8][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t total = (int64_t)27 * cout * cin;
-    if (e >= total) return;
-    const int tap = (int)(e / ((int64_t)cout * cin));
-    const int co = (int)((e / cin) % cout), ci = (int)(e % cin);
+    const int64_t e = (int64_t)blockIdx.x * 32 + lane;
     float s = 0.f;
-    for (int c = 0; c < nchunk; ++c) s += part[((int64_t)c * 27 + tap) * cout * cin + (int64_t)co * cin + ci];
-    dw[((int64_t)co * 27 + tap) * cin + ci] = s;
+    if (e < total) {
+#pragma unroll 8
+        for (int c = warp; c < nchunk; c += 8) s += part[(int64_t)c * total + e];
+    }
+    s_part[warp][lane] = s;
+    __syncthreads();
+    if (warp == 0 && e < total) {
+        float t = 0.f;
+#pragma unroll
+        for (int w = 0; w < 8; ++w) t += s_part[w][lane];
+        const int tap = (int)(e / ((int64_t)cout * cin));
+        const int co = (int)((e / cin) % cout), ci = (int)(e % cin);
+        dw[((int64_t)co * 27 + tap) * cin + ci] = t;
+    }
 }
 
-// db[co] = sum over chunks (fixed order) of dbpart[chunk][co].
-__global__ void bias_reduce_kernel(const float* __restrict__ dbpart, float* __restrict__ db, int nchunk, int cout) {
-    const int co = blockIdx.x * blockDim.x + threadIdx.x;
-    if (co >= cout) return;
+// db[co] = sum over chunks of dbpart[chunk][co], in the same fixed warp-split order.
+__global__ void __launch_bounds__(256) bias_reduce_kernel(const float* __restrict__ dbpart, float* __restrict__ db,
+                                                           int nchunk, int cout) {
+    __shared__ float s_part[8][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int co = blockIdx.x * 32 + lane;
     float s = 0.f;
-    for (int c = 0; c < nchunk; ++c) s += dbpart[(int64_t)c * cout + co];
-    db[co] = s;
+    if (co < cout) {
+#pragma unroll 8
+        for (int c = warp; c < nchunk; c += 8) s += dbpart[(int64_t)c * cout + co];
+    }
+    s_part[warp][lane] = s;
+    __syncthreads();
+    if (warp == 0 && co < cout) {
+        float t = 0.f;
+#pragma unroll
+        for (int w = 0; w < 8; ++w) t += s_part[w][lane];
+        db[co] = t;
+    }
 }
 
 // wt[ci][tap][co] = w[co][26 - tap][ci]
@@ -281,7 +306,8 @@ int check(const char* what) {
 extern "C" {
 
 int64_t lbm_nn_wgrad_scratch_floats(int32_t n, int32_t d, int32_t h, int32_t w, int32_t cin, int32_t cout) {
-    const int64_t chunks = std::max(nn_wgrad_tc_chunks((int64_t)n * d * h * w), nn_wgrad_tma_chunks(n, d, h, w));
+    const int64_t chunks = std::max(std::max(nn_wgrad_tc_chunks((int64_t)n * d * h * w), nn_wgrad_tma_chunks(n, d, h, w)),
+                                    nn_wgrad_ws_chunks(n, d, h, w));
     return chunks * (27 * (int64_t)cin * cout + cout);
 }
 
@@ -292,16 +318,19 @@ int lbm_nn_conv3d_wgrad(const void* in, const void* g, float* dw, float* db, flo
     if (scratch_floats < lbm_nn_wgrad_scratch_floats(n, d, h, w, cin, cout))
         return lbm_set_err(nullptr, LBM_EINVAL, "lbm_nn_conv3d_wgrad: scratch too small");
     cudaStream_t s = (cudaStream_t)stream;
-    const bool tma = nn_wgrad_tma_usable(cin, cout);
-    const int nchunk = (int)(tma ? nn_wgrad_tma_chunks(n, d, h, w) : nn_wgrad_tc_chunks(nvox));
+    const bool ws = nn_wgrad_ws_usable(cin, cout);
+    const bool tma = !ws && nn_wgrad_tma_usable(cin, cout);
+    const int nchunk = (int)(ws ? nn_wgrad_ws_chunks(n, d, h, w)
+                                : (tma ? nn_wgrad_tma_chunks(n, d, h, w) : nn_wgrad_tc_chunks(nvox)));
     float* dbpart = scratch + (int64_t)nchunk * 27 * cin * cout;
-    int rc = tma ? nn_wgrad_tma(in, g, scratch, dbpart, n, d, h, w, cin, cout, s)
-                 : nn_wgrad_tc_launch(in, g, scratch, dbpart, n, d, h, w, cin, cout, s);
+    int rc = ws    ? nn_wgrad_ws(in, g, scratch, dbpart, n, d, h, w, cin, cout, s)
+             : tma ? nn_wgrad_tma(in, g, scratch, dbpart, n, d, h, w, cin, cout, s)
+                   : nn_wgrad_tc_launch(in, g, scratch, dbpart, n, d, h, w, cin, cout, s);
     if (rc) return rc;
-    wgrad_reduce_kernel<<<blocks((int64_t)27 * cin * cout), 256, 0, s>>>(scratch, dw, nchunk, cin, cout);
+    wgrad_reduce_kernel<<<(unsigned)(((int64_t)27 * cin * cout + 31) / 32), 256, 0, s>>>(scratch, dw, nchunk, cin, cout);
     rc = check("wgrad_reduce_kernel");
     if (rc || !db) return rc;
-    bias_reduce_kernel<<<blocks(cout), 256, 0, s>>>(dbpart, db, nchunk, cout);
+    bias_reduce_kernel<<<(unsigned)((cout + 31) / 32), 256, 0, s>>>(dbpart, db, nchunk, cout);
     return check("bias_reduce_kernel");
 }
 
