@@ -226,6 +226,207 @@ __global__ void act_bwd_kernel(bf16* __restrict__ g, const bf16* __restrict__ d,
 }
 
 // Head weight/bias gradient partials per block: part[block][o*cin + c], part[block][cout*cin + o].
+// ---- 16-byte (8-channel) forms of the memory kernels above, for channel counts that are
+// multiples of 8: the same per-element arithmetic in the same order, one vector per thread.
+union V8 {
+    uint4 u;
+    bf16 h[8];
+};
+
+// The vector forms need 16-byte aligned tensors (8-byte for the pool argmax); NULL passes.
+__host__ inline bool al16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+__host__ inline bool al8(const void* p) { return ((uintptr_t)p & 7u) == 0; }
+
+__global__ void concat8_kernel(const uint4* __restrict__ a, int ca8, const uint4* __restrict__ b, int cb8,
+                               uint4* __restrict__ out, int64_t nvox) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int C8 = ca8 + cb8;
+    if (e >= nvox * C8) return;
+    const int64_t v = e / C8;
+    const int c = (int)(e - v * C8);
+    out[e] = c < ca8 ? a[v * ca8 + c] : b[v * cb8 + (c - ca8)];
+}
+
+__global__ void split8_kernel(const uint4* __restrict__ g, int ca8, int cb8, uint4* __restrict__ ga, uint4* __restrict__ gb,
+                              const uint4* __restrict__ mask_b, int accumulate_b, int64_t nvox) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int C8 = ca8 + cb8;
+    if (e >= nvox * C8) return;
+    const int64_t v = e / C8;
+    const int c = (int)(e - v * C8);
+    if (c < ca8) {
+        ga[v * ca8 + c] = g[e];
+        return;
+    }
+    const int64_t o = v * cb8 + (c - ca8);
+    V8 in, acc, m, r;
+    in.u = g[e];
+    if (accumulate_b) acc.u = gb[o];
+    if (mask_b) m.u = mask_b[o];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        float val = __bfloat162float(in.h[q]);
+        if (accumulate_b) val += __bfloat162float(acc.h[q]);
+        if (mask_b && !(__bfloat162float(m.h[q]) > 0.f)) val = 0.f;
+        r.h[q] = __float2bfloat16_rn(val);
+    }
+    gb[o] = r.u;
+}
+
+__global__ void upsample8_kernel(const uint4* __restrict__ in, uint4* __restrict__ out, int N, int d, int h, int w,
+                                 int C8) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t total = (int64_t)N * 8 * d * h * w * C8;
+    if (e >= total) return;
+    const int64_t vo = e / C8;
+    const int c = (int)(e - vo * C8);
+    const Vox P = decode(vo, 2 * d, 2 * h, 2 * w);
+    out[e] = in[((((int64_t)P.n * d + P.z / 2) * h + P.y / 2) * w + P.x / 2) * C8 + c];
+}
+
+__global__ void upsample8_bwd_kernel(const uint4* __restrict__ gout, uint4* __restrict__ gin,
+                                     const uint4* __restrict__ mask, int N, int d, int h, int w, int C8) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t total = (int64_t)N * d * h * w * C8;
+    if (e >= total) return;
+    const int64_t vi = e / C8;
+    const int c = (int)(e - vi * C8);
+    const Vox P = decode(vi, d, h, w);
+    float s[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) s[q] = 0.f;
+    for (int k = 0; k < 8; ++k) {
+        const int z = 2 * P.z + (k >> 2), y = 2 * P.y + ((k >> 1) & 1), x = 2 * P.x + (k & 1);
+        V8 g;
+        g.u = gout[((((int64_t)P.n * 2 * d + z) * 2 * h + y) * 2 * w + x) * C8 + c];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) s[q] += __bfloat162float(g.h[q]);
+    }
+    V8 m, r;
+    if (mask) m.u = mask[e];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        float val = s[q];
+        if (mask && !(__bfloat162float(m.h[q]) > 0.f)) val = 0.f;
+        r.h[q] = __float2bfloat16_rn(val);
+    }
+    gin[e] = r.u;
+}
+
+__global__ void pool8_kernel(const uint4* __restrict__ in, uint4* __restrict__ out, uint2* __restrict__ arg, int N, int D,
+                             int H, int W, int C8) {
+    const int d = D / 2, h = H / 2, w = W / 2;
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t total = (int64_t)N * d * h * w * C8;
+    if (e >= total) return;
+    const int64_t vo = e / C8;
+    const int c = (int)(e - vo * C8);
+    const Vox P = decode(vo, d, h, w);
+    float best[8];
+    int bi[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        best[q] = -3.0e38f;
+        bi[q] = 0;
+    }
+    for (int k = 0; k < 8; ++k) {
+        const int z = 2 * P.z + (k >> 2), y = 2 * P.y + ((k >> 1) & 1), x = 2 * P.x + (k & 1);
+        V8 v;
+        v.u = in[((((int64_t)P.n * D + z) * H + y) * W + x) * C8 + c];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const float val = __bfloat162float(v.h[q]);
+            if (val > best[q]) {
+                best[q] = val;
+                bi[q] = k;
+            }
+        }
+    }
+    V8 r;
+    uint32_t a0 = 0, a1 = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        r.h[q] = __float2bfloat16_rn(best[q]);
+        if (q < 4) a0 |= (uint32_t)bi[q] << (8 * q);
+        else a1 |= (uint32_t)bi[q] << (8 * (q - 4));
+    }
+    out[e] = r.u;
+    arg[e] = make_uint2(a0, a1);
+}
+
+__global__ void pool8_bwd_kernel(const uint4* __restrict__ gout, const uint2* __restrict__ arg, uint4* __restrict__ gin,
+                                 const uint4* __restrict__ mask, int N, int D, int H, int W, int C8, int accumulate) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t total = (int64_t)N * D * H * W * C8;
+    if (e >= total) return;
+    const int64_t vi = e / C8;
+    const int c = (int)(e - vi * C8);
+    const Vox P = decode(vi, D, H, W);
+    const int d = D / 2, h = H / 2, w = W / 2;
+    const int64_t o = ((((int64_t)P.n * d + P.z / 2) * h + P.y / 2) * w + P.x / 2) * C8 + c;
+    const int k = ((P.z & 1) << 2) | ((P.y & 1) << 1) | (P.x & 1);
+    const uint2 a = arg[o];
+    V8 g, acc, m, r;
+    g.u = gout[o];
+    if (accumulate) acc.u = gin[e];
+    if (mask) m.u = mask[e];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const int aq = (int)(((q < 4 ? a.x : a.y) >> (8 * (q & 3))) & 0xFFu);
+        float val = aq == k ? __bfloat162float(g.h[q]) : 0.f;
+        if (accumulate) val += __bfloat162float(acc.h[q]);
+        if (mask && !(__bfloat162float(m.h[q]) > 0.f)) val = 0.f;
+        r.h[q] = __float2bfloat16_rn(val);
+    }
+    gin[e] = r.u;
+}
+
+// Head weight gradient for the network's 1x1 head (16 -> 4) in one pass: each thread
+// accumulates all 68 sums over a grid-stride set of voxels, then a fixed tree (warp
+// shuffles, then the 8 warps in order) gives the block's partial.
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(256) head_wgrad1_kernel(const float* __restrict__ gy, const bf16* __restrict__ x,
+                                                         float* __restrict__ part, int64_t nvox) {
+    constexpr int NOUT = COUT * CIN + COUT;
+    __shared__ float sh[8][NOUT];
+    float acc[NOUT];
+#pragma unroll
+    for (int k = 0; k < NOUT; ++k) acc[k] = 0.f;
+    for (int64_t v = (int64_t)blockIdx.x * 256 + threadIdx.x; v < nvox; v += (int64_t)gridDim.x * 256) {
+        float g[COUT], xv[CIN];
+#pragma unroll
+        for (int o = 0; o < COUT; ++o) g[o] = gy[v * COUT + o];
+#pragma unroll
+        for (int c8 = 0; c8 < CIN / 8; ++c8) {
+            V8 t;
+            t.u = reinterpret_cast<const uint4*>(x + v * CIN)[c8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) xv[c8 * 8 + q] = __bfloat162float(t.h[q]);
+        }
+#pragma unroll
+        for (int o = 0; o < COUT; ++o) {
+#pragma unroll
+            for (int c = 0; c < CIN; ++c) acc[o * CIN + c] += g[o] * xv[c];
+            acc[COUT * CIN + o] += g[o];
+        }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NOUT; ++k) {
+        float t = acc[k];
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
+        if (lane == 0) sh[warp][k] = t;
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < NOUT; k += 256) {
+        float t = 0.f;
+#pragma unroll
+        for (int w8 = 0; w8 < 8; ++w8) t += sh[w8][k];
+        part[(int64_t)blockIdx.x * NOUT + k] = t;
+    }
+}
+
 __global__ void __launch_bounds__(256) head_wgrad_kernel(const float* __restrict__ gy, const bf16* __restrict__ x,
                                                          float* __restrict__ part, int64_t nvox, int cin, int cout) {
     __shared__ float sh[256];
@@ -343,6 +544,11 @@ int lbm_nn_flip_transpose(const void* w, void* wt, int32_t cin, int32_t cout, vo
 int lbm_nn_pool2(const void* in, void* out, uint8_t* arg, int32_t n, int32_t d, int32_t h, int32_t w, int32_t c,
                  void* stream) {
     if ((d | h | w) & 1) return lbm_set_err(nullptr, LBM_EINVAL, "lbm_nn_pool2: even sizes required");
+    if (c % 8 == 0 && al16(in) && al16(out) && al8(arg)) {
+        pool8_kernel<<<blocks((int64_t)n * (d / 2) * (h / 2) * (w / 2) * (c / 8)), 256, 0, (cudaStream_t)stream>>>(
+            (const uint4*)in, (uint4*)out, (uint2*)arg, n, d, h, w, c / 8);
+        return check("pool8_kernel");
+    }
     pool2_kernel<<<blocks((int64_t)n * (d / 2) * (h / 2) * (w / 2) * c), 256, 0, (cudaStream_t)stream>>>(
         (const bf16*)in, (bf16*)out, arg, n, d, h, w, c);
     return check("pool2_kernel");
@@ -350,12 +556,22 @@ int lbm_nn_pool2(const void* in, void* out, uint8_t* arg, int32_t n, int32_t d, 
 
 int lbm_nn_pool2_bwd(const void* gout, const uint8_t* arg, void* gin, const void* mask, int32_t n, int32_t d,
                      int32_t h, int32_t w, int32_t c, int32_t accumulate, void* stream) {
+    if (c % 8 == 0 && al16(gout) && al8(arg) && al16(gin) && al16(mask)) {
+        pool8_bwd_kernel<<<blocks((int64_t)n * d * h * w * (c / 8)), 256, 0, (cudaStream_t)stream>>>(
+            (const uint4*)gout, (const uint2*)arg, (uint4*)gin, (const uint4*)mask, n, d, h, w, c / 8, accumulate);
+        return check("pool8_bwd_kernel");
+    }
     pool2_bwd_kernel<<<blocks((int64_t)n * d * h * w * c), 256, 0, (cudaStream_t)stream>>>(
         (const bf16*)gout, arg, (bf16*)gin, (const bf16*)mask, n, d, h, w, c, accumulate);
     return check("pool2_bwd_kernel");
 }
 
 int lbm_nn_upsample2(const void* in, void* out, int32_t n, int32_t d, int32_t h, int32_t w, int32_t c, void* stream) {
+    if (c % 8 == 0 && al16(in) && al16(out)) {
+        upsample8_kernel<<<blocks((int64_t)n * 8 * d * h * w * (c / 8)), 256, 0, (cudaStream_t)stream>>>(
+            (const uint4*)in, (uint4*)out, n, d, h, w, c / 8);
+        return check("upsample8_kernel");
+    }
     upsample2_kernel<<<blocks((int64_t)n * 8 * d * h * w * c), 256, 0, (cudaStream_t)stream>>>((const bf16*)in,
                                                                                                 (bf16*)out, n, d, h, w, c);
     return check("upsample2_kernel");
@@ -363,12 +579,22 @@ int lbm_nn_upsample2(const void* in, void* out, int32_t n, int32_t d, int32_t h,
 
 int lbm_nn_upsample2_bwd(const void* gout, void* gin, const void* mask, int32_t n, int32_t d, int32_t h, int32_t w,
                          int32_t c, void* stream) {
+    if (c % 8 == 0 && al16(gout) && al16(gin) && al16(mask)) {
+        upsample8_bwd_kernel<<<blocks((int64_t)n * d * h * w * (c / 8)), 256, 0, (cudaStream_t)stream>>>(
+            (const uint4*)gout, (uint4*)gin, (const uint4*)mask, n, d, h, w, c / 8);
+        return check("upsample8_bwd_kernel");
+    }
     upsample2_bwd_kernel<<<blocks((int64_t)n * d * h * w * c), 256, 0, (cudaStream_t)stream>>>(
         (const bf16*)gout, (bf16*)gin, (const bf16*)mask, n, d, h, w, c);
     return check("upsample2_bwd_kernel");
 }
 
 int lbm_nn_concat(const void* a, int32_t ca, const void* b, int32_t cb, void* out, int64_t nvox, void* stream) {
+    if (ca % 8 == 0 && cb % 8 == 0 && al16(a) && al16(b) && al16(out)) {
+        concat8_kernel<<<blocks(nvox * ((ca + cb) / 8)), 256, 0, (cudaStream_t)stream>>>(
+            (const uint4*)a, ca / 8, (const uint4*)b, cb / 8, (uint4*)out, nvox);
+        return check("concat8_kernel");
+    }
     concat_kernel<<<blocks(nvox * (ca + cb)), 256, 0, (cudaStream_t)stream>>>((const bf16*)a, ca, (const bf16*)b, cb,
                                                                               (bf16*)out, nvox);
     return check("concat_kernel");
@@ -376,6 +602,11 @@ int lbm_nn_concat(const void* a, int32_t ca, const void* b, int32_t cb, void* ou
 
 int lbm_nn_split(const void* g, int32_t ca, int32_t cb, void* ga, void* gb, const void* mask_b, int32_t accumulate_b,
                  int64_t nvox, void* stream) {
+    if (ca % 8 == 0 && cb % 8 == 0 && al16(g) && al16(ga) && al16(gb) && al16(mask_b)) {
+        split8_kernel<<<blocks(nvox * ((ca + cb) / 8)), 256, 0, (cudaStream_t)stream>>>(
+            (const uint4*)g, ca / 8, cb / 8, (uint4*)ga, (uint4*)gb, (const uint4*)mask_b, accumulate_b, nvox);
+        return check("split8_kernel");
+    }
     split_kernel<<<blocks(nvox * (ca + cb)), 256, 0, (cudaStream_t)stream>>>(
         (const bf16*)g, ca, cb, (bf16*)ga, (bf16*)gb, (const bf16*)mask_b, accumulate_b, nvox);
     return check("split_kernel");
@@ -404,7 +635,10 @@ int lbm_nn_head_bwd_act(const float* gy, const float* w, const void* x, const vo
     int rc = check("head_bwd_data_kernel");
     if (rc) return rc;
     const int nb = 256, nout = cout * cin + cout;
-    head_wgrad_kernel<<<nb, 256, 0, s>>>(gy, (const bf16*)x, scratch, nvox, cin, cout);
+    if (cin == 16 && cout == 4 && al16(x))
+        head_wgrad1_kernel<16, 4><<<nb, 256, 0, s>>>(gy, (const bf16*)x, scratch, nvox);
+    else
+        head_wgrad_kernel<<<nb, 256, 0, s>>>(gy, (const bf16*)x, scratch, nvox, cin, cout);
     rc = check("head_wgrad_kernel");
     if (rc) return rc;
     sum_partials_kernel<<<blocks(nout), 256, 0, s>>>(scratch, dw_db, nb, nout);
