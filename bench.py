@@ -513,6 +513,51 @@ def unet_step(steps=10, warmup=3, n=2, edge=96, activation="relu"):
 UNET_LAYER_SHAPES = [(16, 16, 0), (16, 32, 1), (32, 32, 1), (32, 64, 2), (64, 64, 2), (96, 32, 1), (48, 16, 0)]
 
 
+# wider convolutions than the network's, for the kernels' ceiling: (cin, cout) on n x edge^3
+UNET_WIDE_SHAPES = [(64, 64), (96, 96), (128, 96), (64, 96), (96, 64), (128, 64)]
+
+
+def unet_wide(n=2, edge=96, iters=10):
+    """Forward 3x3x3 convolutions (ReLU epilogue) wider than the network's layers, each timed
+    alone with CUDA events: TFLOP/s of 2 x voxels x 27 x cin x cout, against the measured
+    bf16 peak."""
+    import ctypes
+    import torch
+    from taichi_lbm3d_gb300 import unet
+    L = unet._lib()
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    peak = None
+    try:
+        with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")) as f:
+            peak = float(json.load(f)["bf16_tflops"])
+    except (OSError, KeyError, ValueError):
+        pass
+    rows = []
+    torch.manual_seed(0)
+    for cin, cout in UNET_WIDE_SHAPES:
+        x = torch.randn((n, edge, edge, edge, cin), device="cuda").to(torch.bfloat16)
+        w = (torch.randn((cout, 27, cin), device="cuda") / (27 * cin) ** 0.5).to(torch.bfloat16)
+        b = torch.randn(cout, device="cuda")
+        y = torch.empty((n, edge, edge, edge, cout), device="cuda", dtype=torch.bfloat16)
+        f = lambda: L.lbm_nn_conv3d_act(p(x), p(w), p(b), None, p(y), None, n, edge, edge, edge, cin, cout, 0, s)
+        for _ in range(3):
+            assert f() == 0
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(iters):
+            f()
+        e1.record()
+        e1.synchronize()
+        us = e0.elapsed_time(e1) / iters * 1e3
+        tf = 2.0 * n * edge ** 3 * 27 * cin * cout / us / 1e6
+        rows.append({"cin": cin, "cout": cout, "us": us, "tflops": tf,
+                     "frac_of_bf16_peak": tf / peak if peak else None})
+        del x, w, b, y
+    return {"workload": "forward 3x3x3 convolutions, %d x %d^3, random data" % (n, edge), "layers": rows}
+
+
 def unet_layers(n=2, edge=96, iters=20):
     """Per-layer 3x3x3 convolution kernels of the warm-start network on n x edge^3:
     forward (ReLU epilogue), backward-data (the transposed shape, masked
@@ -698,6 +743,8 @@ def main():
     ap.add_argument("--unet", action="store_true", help="warm-start U-Net training step on 2 x 96^3")
     ap.add_argument("--unet-layers", action="store_true",
                     help="each U-Net convolution kernel (forward, backward-data, weight gradient) timed alone")
+    ap.add_argument("--unet-wide", action="store_true",
+                    help="forward convolutions wider than the network's (64-128 channels) timed alone")
     ap.add_argument("--cavity", action="store_true", help="64^3 lid-driven cavity, GPU vs CPU oracle")
     a = ap.parse_args()
     if a.cavity:
@@ -708,6 +755,9 @@ def main():
         return 0
     if a.unet_layers:
         print(json.dumps({"unet_layers": unet_layers(iters=a.steps or 20)}))
+        return 0
+    if a.unet_wide:
+        print(json.dumps({"unet_wide": unet_wide(iters=a.steps or 10)}))
         return 0
     if a.unet:
         print(json.dumps({"unet": unet_step(steps=a.steps or 10),
