@@ -1,5 +1,14 @@
-// 3x3x3 convolution of the warm-start network with its operands moved by the
-// tensor memory accelerator (TMA) and multiplied by tcgen05.mma.
+// 3x3x3 convolutions of the warm-start network on tcgen05.mma with operands
+// moved by the tensor memory accelerator (TMA) or from a shared-memory halo.
+// Four kernels, chosen per layer shape by lbm_nn_conv3d_act /
+// lbm_nn_conv3d_wgrad (nn_tc.cu, nn_unet.cu):
+//   conv3d_tma_kernel        forward / backward-data, im2col TMA loads per tap
+//   conv3d_halo_kernel       forward / backward-data of narrow layers, one halo
+//                            and all weights per CTA, taps as descriptor offsets
+//   conv3d_wgrad_tma_kernel  weight gradient from tiled TMA boxes (MN-major)
+//   conv3d_wgrad_ws_kernel   weight gradient, warp-specialised: one halo box per
+//                            block, copy warps build the tap slots
+// Each kernel's own comment describes its layout.  The first:
 //
 // Implicit GEMM as in nn_tc.cu (M = 128 consecutive voxels per CTA, one TMEM
 // lane each; N = output channels; K = 27 taps x input channels), but a
