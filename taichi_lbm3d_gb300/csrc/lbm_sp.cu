@@ -47,12 +47,11 @@
 #ifndef LBM_SP_MINBLOCKS_DEV
 #define LBM_SP_MINBLOCKS_DEV 5
 #endif
-// The 16-bit codecs keep each direction's source reference (or the node's own,
-// for bounce-back) live across the population loads and spill at 48
-// registers: 4 CTAs per SM (64 registers) measured FP16 32.0k / BF16 32.5k
-// MLUPS against 29.5k / 30.2k at 5.
+// The 16-bit codecs on the 256^3 pack: 6 CTAs of 256 per SM (40 registers, 16-24
+// bytes spilled) measured FP16 32.2k / BF16 32.8k MLUPS, 4 CTAs (64 registers, no
+// spill) 32.0k / 32.5k, 5 CTAs (48 registers, 68 bytes spilled) 29.5k / 30.2k.
 #ifndef LBM_SP_MINBLOCKS_16
-#define LBM_SP_MINBLOCKS_16 4
+#define LBM_SP_MINBLOCKS_16 6
 #endif
 // Programmatic dependent launch of consecutive steps: each step's CTAs may
 // become resident while the previous step drains and wait (griddepcontrol)
