@@ -35,23 +35,25 @@
 #include "lbm_kernels.cuh"
 
 // Resident 256-thread CTAs per SM requested for the step kernel (caps
-// registers at 65536 / (256 * n)).  The reference-arithmetic FP32 kernel is
-// fastest at 6 (40 registers), 4 with the dense Guo forcing; the
-// deviation-form kernels, whose pair-form transforms keep more values live,
-// spill at 6 and are fastest at 5, forced or not (measured on the 256^3 pack:
-// unforced f32dev +4%, FP16 +8%, BF16 +13% over 6; forced +1%, +7%, +4%
-// over 4).
+// registers at 65536 / (256 * n)), as measured on the 256^3 pack (MLUPS):
+//  * FP32 reference arithmetic: 6 (40 registers); 4 with the dense Guo forcing;
+//  * FP32 deviation form: 6 (40 registers, no spill): 35.3k against 34.9k at 5,
+//    forced 37.1k against 36.9k;
+//  * 16-bit codecs: 6 (40 registers, 16-24 bytes spilled): FP16 32.2k / BF16
+//    32.8k against 32.0k / 32.5k at 4 (64 registers) and 29.5k / 30.2k at 5
+//    (48 registers, 68 bytes spilled); forced, 4 is ahead (33.4k / 34.0k
+//    against 33.3k / 33.8k at 6).
 #ifndef LBM_SP_MINBLOCKS
 #define LBM_SP_MINBLOCKS 6
 #endif
 #ifndef LBM_SP_MINBLOCKS_DEV
-#define LBM_SP_MINBLOCKS_DEV 5
+#define LBM_SP_MINBLOCKS_DEV 6
 #endif
-// The 16-bit codecs on the 256^3 pack: 6 CTAs of 256 per SM (40 registers, 16-24
-// bytes spilled) measured FP16 32.2k / BF16 32.8k MLUPS, 4 CTAs (64 registers, no
-// spill) 32.0k / 32.5k, 5 CTAs (48 registers, 68 bytes spilled) 29.5k / 30.2k.
 #ifndef LBM_SP_MINBLOCKS_16
 #define LBM_SP_MINBLOCKS_16 6
+#endif
+#ifndef LBM_SP_MINBLOCKS_16F
+#define LBM_SP_MINBLOCKS_16F 4
 #endif
 // Programmatic dependent launch of consecutive steps: each step's CTAs may
 // become resident while the previous step drains and wait (griddepcontrol)
@@ -114,7 +116,7 @@ __device__ __forceinline__ void sp_finish_node(typename Codec<STORE>::R* F, int 
 
 template <int STORE, bool FORCE, bool MACROS>
 __global__ void __launch_bounds__(256, STORE == LBM_STORE_F64 ? 1
-                                           : Codec<STORE>::RHOREF ? LBM_SP_MINBLOCKS_16
+                                           : Codec<STORE>::RHOREF ? (FORCE ? LBM_SP_MINBLOCKS_16F : LBM_SP_MINBLOCKS_16)
                                        : Codec<STORE>::DEV    ? LBM_SP_MINBLOCKS_DEV
                                            : FORCE                ? 4
                                                                   : LBM_SP_MINBLOCKS)
@@ -286,7 +288,7 @@ __device__ __forceinline__ void spt_next(const SptArgs& A, int nx, int ny, int n
 
 template <int STORE, bool FORCE, bool MACROS>
 __global__ void __launch_bounds__(SPT, STORE == LBM_STORE_F64 ? 1
-                                       : Codec<STORE>::RHOREF ? LBM_SP_MINBLOCKS_16
+                                       : Codec<STORE>::RHOREF ? (FORCE ? LBM_SP_MINBLOCKS_16F : LBM_SP_MINBLOCKS_16)
                                        : Codec<STORE>::DEV    ? LBM_SP_MINBLOCKS_DEV
                                        : FORCE                ? 4
                                                               : LBM_SP_MINBLOCKS)
@@ -383,7 +385,7 @@ __global__ void __launch_bounds__(SPT, STORE == LBM_STORE_F64 ? 1
 // drain for the CTAs resident by then.
 template <int STORE, bool FORCE, bool MACROS>
 __global__ void __launch_bounds__(SPT, STORE == LBM_STORE_F64 ? 1
-                                       : Codec<STORE>::RHOREF ? LBM_SP_MINBLOCKS_16
+                                       : Codec<STORE>::RHOREF ? (FORCE ? LBM_SP_MINBLOCKS_16F : LBM_SP_MINBLOCKS_16)
                                        : Codec<STORE>::DEV    ? LBM_SP_MINBLOCKS_DEV
                                        : FORCE                ? 4
                                                               : LBM_SP_MINBLOCKS)
